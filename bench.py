@@ -1,0 +1,381 @@
+#!/usr/bin/env python3
+"""Movie-registration benchmark: K2-size movies through alignImageStack.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (the K2 configuration): 40 frames of 3838 x 3710 uint8 counts
+(Poisson mean 0.8 e/px/frame) with a U(0.9, 1.1) float32 gain map and 0.01 %
+hot pixels at 50x the mean, random-walk drift 1.2 px/frame; padded to 4096,
+Fourier-cropped to 2048 for the all-pairs triangle (780 pairs, maxShift 100),
+hot-pixel filter, Lanczos shift and sum, lazy even/odd FRC and the dose
+filter at 1.2 e/A^2/frame, 1.05 A/px.  Inputs are seeded synthetic movies.
+
+One step registers one movie.  ``value`` is movies/s with the raw frames
+already resident in HBM; ``e2e`` is the same through the public API from
+pinned host memory (frames and gain copied in, sums, FRC and trajectory
+copied out, every step).  The input (570 MB of frames) is larger than L2.
+Under torchrun each rank registers its own movies (replicas, no collective
+on the data path); ``value`` is the job total.
+
+``--impl reference`` times the reference algorithm on the host cores: the
+float32 CPU restatement of the same pipeline (NumPy/SciPy, FFTs on all
+cores), on a bounded sample of each movie, scaled to a whole movie.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+K2_DOSE = [1.2 * 1.05 ** 2, 0.24499, -1.6649, 2.8141, 32, 0]
+WORKLOADS = {
+    "k2": dict(movie=dict(n_frames=40, shape=(3838, 3710), seed=2024, mean_dose=0.8, drift_sigma=1.2, dtype="uint8",
+                          gain_map=True, hot_fraction=1e-4, hot_factor=50.0),
+               attrs=dict(triMode="tri", shapePadded=[4096, 4096], fouCrop=[2048, 2048], maxShift=100,
+                          pixelsize=0.105, voltage=300.0, filterMode="hot,dose", doseFiltParam=K2_DOSE,
+                          subPixReg=16, shiftMethod="lanczos", Bmode="opti", doLazyFRC=True)),
+    "small": dict(movie=dict(n_frames=20, shape=(1024, 1024), seed=1, mean_dose=1.0, drift_sigma=0.8),
+                  attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[1024, 1024], maxShift=40,
+                             pixelsize=0.1, voltage=300.0, filterMode="dose",
+                             doseFiltParam=[1.0, 0.24499, -1.6649, 2.8141, 32, 0], subPixReg=16)),
+}
+METRIC = "4k x 4k x 40 movies/sec (K2 3838x3710x40 registration)"
+UNIT = "movies/s"
+
+
+def algorithmic_bytes(N, H, W, C, w, M, b_in):
+    """Unique logical bytes per movie and stage: every input element read once,
+    every output written once (FFT intermediates excluded)."""
+    HW = H * W
+    spec = C * (C // 2 + 1) * 8
+    return {"A_gain_sum": N * HW * b_in + 8 * HW, "B_hot_maps": 12 * HW,
+            "C_spectra": N * HW * b_in + 12 * HW + 2 * N * spec, "D_frame_terms": 2 * N * spec + 16 * N * w * w,
+            "E_pairs": N * spec + 4 * M * w * w, "F_peaks": 4 * M * w * w, "G_shift_sum": N * HW * b_in + 24 * HW,
+            "H_frc": 8 * HW, "I_dose": N * HW * b_in + 16 * HW}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+
+def cpu_sample(mv, attrs, workers, pairs=2, frames=1, full_steps=False):
+    """Time the float32 CPU restatement (the reference's algorithm) on a
+    bounded sample of one movie and scale it to the whole movie.
+
+    Sample: the hot-pixel filter on the whole stack once (when full_steps),
+    the forward spectra of ``frames`` frames, ``pairs`` pair correlations with
+    their peak search, and the shift, FRC-sum and dose-filter work of
+    ``frames`` frames.  Per-movie time = hot + N*spectra + M*pair + N*(shift +
+    dose) + solve."""
+    from oracle import zorro_oracle as zo
+    dt = zo.Dtypes(False, workers)
+    N, H, W = mv["images"].shape
+    P = attrs["shapePadded"]
+    sC = zo.shape_cropped(attrs["fouCrop"])
+    mS = attrs["maxShift"]
+    tri = zo.tri_indices(N, attrs["triMode"], attrs.get("diagWidth", 5), 0)
+    M = int(tri.sum())
+    imgs = mv["images"][:max(frames, 2)].astype(np.float32)
+    t = {}
+    t0 = time.perf_counter()
+    if full_steps and "hot" in (attrs.get("filterMode") or ""):
+        zo.hotpix_filter(mv["images"], dict(zo.DEFAULTS["hotpixInfo"]), dt=dt)
+    t["hot"] = time.perf_counter() - t0
+    padded, mask = zo.pad_stack(imgs, P)
+    t0 = time.perf_counter()
+    GM, MP = zo.mask_spectrum(mask, sC, dt)
+    spec = [zo.frame_spectra(padded[i], mask, sC, dt) for i in range(max(frames, 2))]
+    t["spectra_per_frame"] = (time.perf_counter() - t0) / max(frames, 2)
+    nc2 = zo.norm_const2(sC)
+    mmask = zo.max_shift_mask(mS)
+    t0 = time.perf_counter()
+    for _ in range(pairs):
+        Cw, _ = zo.mnxc2(spec[0][0], spec[0][1], spec[1][0], spec[1][1], GM, MP, nc2, mS, True, dt)
+        zo.locate_peak(Cw, mmask, attrs.get("subPixReg", 16), "opti", dt=dt)
+    t["pair"] = (time.perf_counter() - t0) / pairs
+    trans = np.zeros((frames, 2)) + 0.3
+    t0 = time.perf_counter()
+    zo.apply_shifts(imgs[:frames].copy(), trans, originMode=None)
+    t["shift_per_frame"] = (time.perf_counter() - t0) / frames
+    t0 = time.perf_counter()
+    if "dose" in (attrs.get("filterMode") or ""):
+        zo.dose_filter(imgs[:frames], P, attrs["pixelsize"], 300.0, attrs["doseFiltParam"],
+                       np.zeros((H, W), np.float32), dt=dt)
+    t["dose_per_frame"] = (time.perf_counter() - t0) / frames
+    movie_s = t["hot"] + N * (t["spectra_per_frame"] + t["shift_per_frame"] + t["dose_per_frame"]) + M * t["pair"]
+    return movie_s, t, "hot-pixel filter of the full stack %s, spectra of %d frames, %d of %d pairs, shift and dose " \
+        "of %d frame(s); scaled to %d frames / %d pairs" % ("(timed)" if full_steps else "(not in sample)",
+                                                             max(frames, 2), pairs, M, frames, N, M)
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return
+    from zorro_gb300.synthetic import make_movie
+    mv = make_movie(**wl["movie"])
+    workers = os.cpu_count() or 1
+    vals = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        s, _, sample = cpu_sample(mv, wl["attrs"], workers, pairs=1, frames=1, full_steps=(i == 0))
+        if i == 0:
+            hot_s = _
+        if i >= args.warmup:
+            vals.append(1.0 / (s + hot_s.get("hot", 0.0)))
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded K2-size movie)",
+            "config": {"workload": args.workload, **{k: wl["attrs"][k] for k in ("triMode", "shapePadded", "fouCrop",
+                                                                              "maxShift", "filterMode")}},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------- GPU arm
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="k2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="run the warm-up and 2 steps, no timing output")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from zorro_gb300.build import build
+    if rank == 0:
+        build()
+    if dist is not None:
+        dist.barrier()
+    from zorro_gb300 import _lib
+    from zorro_gb300.engine import Engine
+    from zorro_gb300.registrator import ImageRegistrator
+    from zorro_gb300.synthetic import make_movie
+
+    mv = make_movie(**dict(wl["movie"], seed=wl["movie"]["seed"] + rank))
+    raw_np = mv["raw"]
+    gain_np = mv["gain"]
+    b_in = raw_np.dtype.itemsize
+    N, H, W = raw_np.shape
+    dev = torch.device("cuda", local)
+    raw_dev = torch.from_numpy(raw_np).to(dev)
+    gain_dev = torch.from_numpy(gain_np).to(dev) if gain_np is not None else None
+    raw_pin = torch.from_numpy(raw_np).pin_memory()
+    gain_pin = torch.from_numpy(gain_np).pin_memory() if gain_np is not None else None
+
+    def make_reg(images, gain, device_out):
+        r = ImageRegistrator()
+        for k, v in wl["attrs"].items():
+            setattr(r, k, v)
+        r.images = images
+        r.gainRef = gain
+        r.keepAlignedImages = False
+        r.returnDeviceArrays = device_out
+        r.device = local
+        return r
+
+    eng = Engine.get(local)
+    lib = _lib.load()
+    for _ in range(args.warmup):
+        make_reg(raw_dev, gain_dev, True).alignImageStack()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing (value), with per-stage events
+    eng.profile = {}
+    launches0 = lib.zr_launch_count()
+    barrier()
+    with ClockSampler(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        ev0.record()
+        last = None
+        for _ in range(args.steps):
+            last = make_reg(raw_dev, gain_dev, True)
+            last.alignImageStack()
+        ev1.record()
+        barrier()
+        wall = time.perf_counter() - t0
+    launches = lib.zr_launch_count() - launches0
+    dev_ms = ev0.elapsed_time(ev1)
+    stage_ms = eng.stage_ms()
+    eng.profile = None
+    t_step = max(dev_ms / 1000.0, 1e-9) / args.steps
+    if dist is not None:
+        tt = torch.tensor([t_step], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = world / t_step
+
+    # ---- end to end through the public API from pinned host memory
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        r = make_reg(raw_pin, gain_pin, False)
+        r.alignImageStack()
+        _ = (r.translations, r.imageSum, r.filtSum, r.FRC)
+    e1.record()
+    barrier()
+    t_e2e = e0.elapsed_time(e1) / 1000.0 / args.steps
+    if dist is not None:
+        tt = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    h2d = raw_np.nbytes + (gain_np.nbytes if gain_np is not None else 0)
+    d2h = 4 * H * W * 2 + 512 * 512 * 4 + 256 * 8 + N * 2 * 8
+
+    # ---- roofline of the dominant stage
+    w = 2 * wl["attrs"]["maxShift"]
+    C = int(wl["attrs"]["fouCrop"][0])
+    M = N * (N - 1) // 2 if wl["attrs"]["triMode"] == "tri" else None
+    ab = algorithmic_bytes(N, H, W, C, w, M, b_in)
+    per_step = {k: v / args.steps for k, v in stage_ms.items()}
+    dom = max(per_step, key=per_step.get)
+    peak, peak_kind = measured_peaks()
+    achieved = ab[dom] / (per_step[dom] / 1000.0) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            traffic = json.load(fh).get(dom)
+    except Exception:
+        pass
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+            "algorithmic_bytes": ab[dom], "stage_ms_per_step": {k: round(v, 3) for k, v in sorted(per_step.items())},
+            "movie_algorithmic_bytes": sum(ab.values()),
+            "movie_frac": round(sum(ab.values()) / t_step / 1e9 / peak, 4)}
+
+    # ---- accuracy on this movie vs the known drift (the float64 oracle comparison is in the tests)
+    tr = np.asarray(last.translations)
+    truth = -(mv["drift"] - mv["drift"].mean(axis=0))
+    rmse_truth = float(np.sqrt(np.mean((tr - truth) ** 2)))
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline and world == 1:
+            workers = os.cpu_count() or 1
+            s, parts, sample = cpu_sample(mv, wl["attrs"], workers, pairs=3, frames=1, full_steps=True)
+            cpu = {"value": 1.0 / s, "unit": UNIT, "cores": workers, "kind": "port", "sample": sample,
+                   "seconds_per_movie": round(s, 2)}
+        line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(t_step * 1000.0, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded K2-size movies)",
+                "config": {"workload": args.workload + ": 40x3838x3710 u8 + gain + 0.01% hot px, P=4096, C=2048, "
+                           "tri 780 pairs, maxShift 100, hot+dose filters, lazy FRC",
+                           "l2": "inputs (570 MB raw frames per movie) larger than L2; no flush",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "e2e": {"value": round(world / t_e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": int(launches),
+                "wall_s_timed": round(wall, 3),
+                "clocks": clk.summary(),
+                "roofline": roof,
+                "accuracy": {"rmse_vs_true_drift_px": round(rmse_truth, 4)},
+                "cpu_baseline": cpu}
+        if not args.profile_only:
+            print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

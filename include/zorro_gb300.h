@@ -1,0 +1,219 @@
+/*
+ * zorro_gb300 -- C ABI of the GB300 (sm_103a) movie-registration hot path.
+ *
+ * The entry points below replace, step by step, the body of
+ * ``ImageRegistrator.alignImageStack`` in LBEM-CH/zorro (zorro/zorro.py:1569)
+ * and the steps it drives.  Each declaration names the reference code it
+ * stands for.  All pointers are DEVICE pointers unless stated otherwise,
+ * all work is enqueued on ``stream`` (a cudaStream_t passed as void*), and no
+ * entry point allocates device memory: scratch space is passed in as
+ * ``work``/``work_bytes`` (query the size with the matching *_work_bytes
+ * function).  Return value: ZR_OK (0) or a negative ZR_E* code; the message
+ * of the last failure on the calling thread is available from
+ * zr_last_error().
+ *
+ * Layouts (row-major, C order):
+ *   frames      [N][H][W] raw counts (see zr_frames_t)
+ *   spectrum    [C0+1][K4] complex float, K4 = zr_spectrum_pitch(C1): rows 0..C0-1
+ *               are the Fourier-cropped frequencies ky in FFT order (row C0/2 holds
+ *               ky = -C0/2), row C0 holds ky = +C0/2; column k holds kx = k for
+ *               0 <= k <= C1/2 (the half-plane of a real image).
+ *   window      [w][w] float, w = 2*max_shift; element (a, b) is the correlation
+ *               at shift (y, x) = (a - max_shift, b - max_shift).
+ */
+#ifndef ZORRO_GB300_H
+#define ZORRO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZR_OK 0
+#define ZR_EINVAL (-1)   /* invalid argument (ValueError in the reference) */
+#define ZR_ECUDA (-2)    /* CUDA runtime error */
+#define ZR_ESIZE (-3)    /* size outside what the kernels support */
+#define ZR_EWORK (-4)    /* scratch buffer too small */
+
+/* raw pixel types */
+#define ZR_F32 0
+#define ZR_U8 1
+#define ZR_U16 2
+#define ZR_F16 3
+
+/* One movie's frames and the per-pixel corrections applied when they are
+ * read: v = float32(gain*raw) (zorro.py:3466), v /= gain_divisor when nonzero
+ * (zorro.py:3477), v = hot_a*v + hot_b (hotpixFilter, zorro.py:2649). */
+typedef struct zr_frames {
+  const void* raw;
+  int raw_type;
+  const float* gain;   /* [H][W] or NULL */
+  const float* hot_a;  /* [H][W] or NULL (then hot_b is ignored) */
+  const float* hot_b;  /* [H][W] */
+  float gain_divisor;  /* 0: none */
+  int n_frames, height, width;
+  long long frame_stride; /* elements between frames, 0 = height*width */
+} zr_frames_t;
+
+/* Hot-pixel filter constants (zorro.py:2595-2649). */
+typedef struct zr_hotpix_params {
+  double mu, sigma;          /* fitted normal CDF of the unaligned sum */
+  float cutoff_lower, cutoff_upper;
+  float logistic_k, relax;
+  float psf[9];              /* normalised 3x3 detector PSF */
+  float neighbour_thres;     /* 0.01 */
+  double best_mean;          /* mu / n_frames */
+} zr_hotpix_params_t;
+
+/* Peak search constants (locatePeak, zorro.py:1099-1231). */
+typedef struct zr_peak_params {
+  int sub_pix_reg;           /* subPixReg */
+  int bmode;                 /* 0 none, 1 'opti', 2 'conv' */
+  int suppress_origin;       /* suppressOrigin */
+  int use_mask;              /* maxShift circular mask */
+  double conv_sigma_y, conv_sigma_x; /* bmode 2 */
+  double opti_lo, opti_hi, opti_xatol; /* 0, 7, 0.01 */
+  int opti_maxiter;          /* 15 */
+} zr_peak_params_t;
+
+typedef struct zr_peak_result {
+  double shift_y, shift_x;   /* in cropped pixels (before the P/C scale) */
+  double sigma;              /* 'opti' Gaussian sigma */
+  float corr, peaksig, origin;
+  int cy, cx;                /* integer peak position in the window */
+  int flags;                 /* bit0: sub-pixel patch hit the window edge */
+  int nfev;
+} zr_peak_result_t;
+
+/* Per-frame shift applied by applyShifts (zorro.py:1774 ->
+ * zorro_util.py:341-379): np.roll by (roll_y, roll_x), then the separable
+ * 3x3 Lanczos kernel ky (x) kx with reflect boundaries (identity when
+ * apply == 0). */
+typedef struct zr_shift {
+  int roll_y, roll_x;
+  int apply;
+  float ky[3], kx[3];
+} zr_shift_t;
+
+/* Dose-filter constants (doseFilter, zorro.py:2375-2452). */
+typedef struct zr_dose_params {
+  float crit_a, crit_b, crit_c;  /* critical-dose curve */
+  float cutoff_order;            /* 32 */
+  float voltage_scaling;         /* sqrt(kV/300) */
+  float inv_ps_x, inv_ps_y;      /* 1/(P*pixelsize_A) */
+  int normalize;                 /* 'dosenorm' */
+} zr_dose_params_t;
+
+int zr_version(void);
+int zr_last_error(char* buf, size_t len);
+
+/* Number of kernels this library has launched in the process (instrumentation;
+ * no counterpart in the reference). */
+unsigned long long zr_launch_count(void);
+
+/* One-time per-device setup (twiddle table).  Replaces the FFTW planning in
+ * zorro_util.py:966-1066 (pyFFTWPlanner). */
+int zr_init(int device);
+
+/* ---- gain and hot pixels: hotpixFilter, zorro.py:2497-2672 ---- */
+
+/* unaligned_sum[y][x] = sum over n (in frame order, float32) of the gain-
+ * corrected frames (zorro.py:2529); *total (double, accumulated) += sum of
+ * all pixels of unaligned_sum.  Hot-pixel maps in ``frames`` are ignored. */
+int zr_gain_sum(const zr_frames_t* frames, float* unaligned_sum, double* total, void* stream);
+
+/* np.histogram(values, edges) for unit-width bins first_edge + i
+ * (zorro.py:2533-2534).  counts[nbins] is accumulated, not cleared. */
+int zr_histogram(const float* values, long long n, double first_edge, int nbins,
+                 unsigned int* counts, void* stream);
+
+/* The logistic masks, PSF fill and neighbour fill of zorro.py:2595-2649,
+ * folded into per-pixel affine maps hot_a (logisticMask) and hot_b
+ * (singletonOutlierMask*psfFiltMean + neighbourFilt).  counts3 (accumulated)
+ * receives guessDeadpix, guessHotpix and neighborPix.  ``work`` holds
+ * zr_hotpix_work_bytes() bytes. */
+size_t zr_hotpix_work_bytes(int height, int width);
+int zr_hotpix_maps(const float* unaligned_sum, int height, int width, int n_frames,
+                   const zr_hotpix_params_t* params, float* hot_a, float* hot_b,
+                   unsigned int* counts3, void* work, size_t work_bytes, void* stream);
+
+/* ---- forward spectra: xcorrnm2_tri, zorro.py:814-925 ---- */
+
+/* sums[n] (double, accumulated) += sum of the corrected frame n over
+ * [0,H)x[0,W).  Used to subtract each frame's mean before the transform
+ * (an exact identity of the masked correlation, see DESIGN). */
+int zr_frame_sums(const zr_frames_t* frames, double* sums, void* stream);
+
+int zr_spectrum_pitch(int C1);
+long long zr_spectrum_elems(int C0, int C1);
+size_t zr_spectra_work_bytes(int height, int n_frames, int C1);
+
+/* Fourier-cropped spectra of frames [frame0, frame0+n_frames): G = FFT(m*I),
+ * S = FFT((m*I)^2) at P0 x P1, cropped to C0 x C1 (zorro.py:875-914).  I is
+ * the corrected frame minus mean_sub[n] (NULL: 0), zero-padded to P0 x P1;
+ * m is ``mask`` ([P0][P1], NULL: ones on [0,H)x[0,W), the padStack mask,
+ * zorro.py:1943-1949).  mode 1 transforms the mask itself into G (S unused),
+ * zorro.py:814-825.  G and S point at the spectrum of frame ``frame0``. */
+int zr_spectra(const zr_frames_t* frames, const float* mask, const double* mean_sub, int frame0,
+               int n_frames, int mode, int P0, int P1, int C0, int C1, void* G, void* S,
+               void* work, size_t work_bytes, void* stream);
+
+/* ---- masked normalised cross-correlation: mnxc2, zorro.py:1014-1097 ---- */
+
+size_t zr_xcorr_work_bytes(int n_jobs, int C1, int max_shift);
+
+/* The frame-only terms of mnxc2, windowed: for every frame n the windows of
+ * CorrTM (template mask), CorrBM (base mask), the two Denominator IFFTs, and
+ * the maskProduct; terms is [4N+1][w][w] (order CTM[0..N), CBM, DT, DB, MP).
+ * zorro.py:1034-1057 and 826-835.  G, S: N spectra each; GM: mask spectrum. */
+int zr_xcorr_terms(const void* G, const void* S, const void* GM, int N, int C0, int C1,
+                   int max_shift, float* terms, void* work, size_t work_bytes, void* stream);
+
+/* The correlation windows C of pairs (I, J) (template I, base J):
+ * numerator IFFT of G_J conj(G_I), combined with the terms as in
+ * zorro.py:1061-1092 (Denom clipped to >= 1), ifftshift-cropped to the
+ * +/-max_shift window.  pairs is [M][2] int (I, J). */
+int zr_xcorr_pairs(const void* G, const float* terms, const int* pairs, int M, int N, int C0, int C1,
+                   int max_shift, float* cwin, void* work, size_t work_bytes, void* stream);
+
+/* ---- peak search: locatePeak, zorro.py:1099-1231 ---- */
+int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr_peak_params_t* params,
+                    zr_peak_result_t* results, void* stream);
+
+/* ---- shift and sum: applyShifts + lazyFouRingCorr sums, zorro.py:1734-1808, 2237-2238 ---- */
+
+/* image_sum = sum_n shifted frame n (float32, frame order); even_sum/odd_sum
+ * likewise over even/odd n (either may be NULL); ``aligned`` [N][H][W]
+ * receives the shifted frames when not NULL.  shifts: device array [N]. */
+int zr_shift_sum(const zr_frames_t* frames, const zr_shift_t* shifts, float* image_sum,
+                 float* even_sum, float* odd_sum, float* aligned, void* stream);
+
+/* ---- tiled FRC: tiledFRC, zorro.py:2246-2310 + rotmean, zorro_util.py:147-224 ---- */
+
+size_t zr_frc_work_bytes(int n_tiles, int box);
+/* offsets: device int array [n_tiles][2] (y, x) of the box x box tiles.  frc2d
+ * [box][box] receives the fftshifted, DC-normalised 2-D FRC; frc [nrings]
+ * (double) its rotational mean. */
+int zr_tiled_frc(const float* even, const float* odd, int height, int width, int box,
+                 const int* offsets, int n_tiles, float* frc2d, double* frc, int nrings,
+                 void* work, size_t work_bytes, void* stream);
+
+/* ---- dose filter: doseFilter, zorro.py:2349-2494 ---- */
+
+size_t zr_dose_work_bytes(int P0, int P1, int n_frames);
+/* filt_sum [H][W] = |IFFT(sum_n FFT(pad_sym(aligned[n])) * thres_n * filt_n)|
+ * cropped to H x W (np.pad 'symmetric' to P0 x P1).  aligned: [N][H][W] the
+ * shifted frames (zr_shift_sum's ``aligned``); thres_q, dose_end: device
+ * float arrays [N] (per-frame cut-off frequency thresQ and accumulated dose
+ * at the end of the frame, zorro.py:2444-2452). */
+int zr_dose_filter(const float* aligned, int N, int H, int W, const zr_dose_params_t* params,
+                   const float* thres_q, const float* dose_end, int P0, int P1, float* filt_sum,
+                   void* work, size_t work_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ZORRO_GB300_H */

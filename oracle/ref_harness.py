@@ -28,8 +28,10 @@ absent or unbuildable here:
   ``sum(w*|A x - b|)`` (``zorro_util.py:849-851``) with the stochastic
   ``scipy.optimize.basinhopping`` (``zorro.py:1415,1422``).  Here that call is
   answered by the exact optimum of the same objective (linear programme,
-  HiGHS).  The logistic fit's basinhopping (``zorro.py:2008``) runs unchanged
-  with a fixed seed.
+  HiGHS).  The logistic fit's basinhopping (``zorro.py:2008``) is answered by
+  the deterministic multi-start minimisation of the same objective and bounds
+  in ``oracle.zorro_oracle.logistic_fit_deterministic`` (basinhopping is
+  chaotic here: 1e-9 changes of its input change the fit by O(1)).
 
 The float dtypes are switched to float64/complex128 after loading, the way
 the reference itself selects them when numexprz is absent (``zorro.py:20-29``).
@@ -72,9 +74,6 @@ _NE_FUNCS = {
     "sqrt": np.sqrt, "exp": np.exp, "log": np.log, "sin": np.sin, "cos": np.cos,
     "arctan2": np.arctan2, "where": np.where,
 }
-
-LOGISTIC_SEED = 1234
-
 
 def _lstsq_strict(a, b, *args, **kw):
     """``np.linalg.lstsq`` as NumPy < 1.14 behaved: empty systems raise."""
@@ -172,8 +171,12 @@ class _SolverShim:
             A, b, w = mk["args"]
             bounds = mk["bounds"]
             return types.SimpleNamespace(x=weighted_l1_exact(A, b, w, bounds))
-        return scipy.optimize.basinhopping(func, x0, niter=niter, minimizer_kwargs=mk,
-                                           rng=np.random.default_rng(LOGISTIC_SEED), **kw)
+        if func is self._util.minLogistic:
+            from oracle.zorro_oracle import logistic_fit_deterministic
+            hSigma, cdf = mk["args"]
+            (lo, hi) = mk["bounds"][0]
+            return types.SimpleNamespace(x=logistic_fit_deterministic(hSigma, cdf, lo, hi, x0[0]))
+        raise RuntimeError("unexpected basinhopping objective %r" % func)
 
 
 def weighted_l1_exact(A, b, w, bounds):

@@ -16,8 +16,9 @@ Parity: pinned against fixtures produced by running the unmodified reference
 (``oracle/ref_harness.py`` via ``tests/golden/make_golden.py``).  Two choices
 are fixed where the reference is stochastic (its shift solve and logistic fit
 use unseeded ``scipy.optimize.basinhopping``): the shift solve returns the
-exact weighted-L1 optimum (linear programme, HiGHS) and the logistic fit runs
-basinhopping with ``LOGISTIC_SEED``.
+exact weighted-L1 optimum (linear programme, HiGHS) and the logistic fit is
+the deterministic multi-start search of ``logistic_fit_deterministic`` on the
+same objective and bounds.
 """
 from __future__ import annotations
 
@@ -280,8 +281,34 @@ def min_logistic(x, hSigma, cdf):
                                            ** np.float64(x[2])))))
 
 
+def _logistic_cdf_error64(x, hSigma, cdf):
+    """min_logistic without its final float32 cast (zorro_util.py:862-863)."""
+    return np.sum(np.abs(cdf - (1.0 - 1.0 / (1.0 + np.exp(-x[1] * (-hSigma + x[0]))) ** x[2])))
+
+
+def logistic_fit_deterministic(hSigma, cdf, lo, hi, mean):
+    """The global minimum of the reference's logistic-CDF error within its
+    bounds (zorro.py:2000-2008), found deterministically: L-BFGS-B from the
+    reference's start point and 27 fixed others, best value wins (earliest
+    start on ties within 1e-9).  The reference's unseeded basinhopping returns
+    a different point every run and jumps between near-equal minima under
+    1e-9 perturbations of its input; this search does not."""
+    bounds = ((lo, hi), (0.1, 20.0), (0.05, 5.0))
+    starts = [(mean, 5.0, 1.0)] + [(lo + f * (hi - lo), K, nu) for f in (0.25, 0.5, 0.75)
+                                   for K in (1.0, 5.0, 12.0) for nu in (0.3, 1.0, 3.0)]
+    best = None
+    for x0 in starts:
+        r = scipy.optimize.minimize(_logistic_cdf_error64, x0, args=(hSigma, cdf), method="L-BFGS-B", bounds=bounds,
+                                    options={"ftol": 1e-15, "gtol": 1e-12, "maxiter": 1000})
+        if best is None or r.fun < best.fun * (1.0 - 1e-9):
+            best = r
+    return best.x
+
+
 def cdf_logistic_curve(peaksigTriMat, seed=LOGISTIC_SEED):
-    """Fit a logistic to the CDF of peak significances.  zorro.py:1981-2022."""
+    """Fit a logistic to the CDF of peak significances.  zorro.py:1981-2022
+    (histogram and objective as the reference; the minimiser is
+    logistic_fit_deterministic)."""
     peaksigs = peaksigTriMat[peaksigTriMat > 0.0]
     bins = int(peaksigs.size / 7.0)
     pdfPeaks, hSigma = np.histogram(peaksigs, bins=bins)
@@ -289,12 +316,8 @@ def cdf_logistic_curve(peaksigTriMat, seed=LOGISTIC_SEED):
     pdfPeaks = pdfPeaks.astype("float32")
     cdfPeaks = np.cumsum(pdfPeaks)
     cdfPeaks /= cdfPeaks[-1]
-    mk = {"bounds": ((np.min(peaksigs), np.max(peaksigs)), (0.1, 20.0), (0.05, 5.0)), "tol": 1e-6,
-          "method": "L-BFGS-B", "args": (hSigma, cdfPeaks)}
-    x0 = [np.mean(peaksigs), 5.0, 1.0]
-    out = scipy.optimize.basinhopping(min_logistic, x0, niter=50, minimizer_kwargs=mk,
-                                      rng=np.random.default_rng(seed))
-    return {"peaksigThres": out.x[0], "logisticK": out.x[1], "logisticNu": out.x[2],
+    x = logistic_fit_deterministic(hSigma, cdfPeaks, np.min(peaksigs), np.max(peaksigs), np.mean(peaksigs))
+    return {"peaksigThres": x[0], "logisticK": x[1], "logisticNu": x[2],
             "pdfPeaks": pdfPeaks, "cdfPeaks": cdfPeaks, "hSigma": hSigma}
 
 

@@ -1,0 +1,118 @@
+"""CPU-only checks: the C ABI library loads and exports every symbol the
+header declares, and the host-side float64 steps of the product agree with
+the oracle.  No kernel is launched here."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import zorro_oracle as zo
+from zorro_gb300 import hostmath as hm
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "zorro_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(zr_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from zorro_gb300 import _lib
+    from zorro_gb300.build import build
+    build()
+    return _lib.load()
+
+
+def test_library_exports_every_header_symbol(lib):
+    from zorro_gb300 import _lib
+    names = header_functions()
+    assert names, "no declarations parsed"
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(_lib.EXPORTS), set(names) ^ set(_lib.EXPORTS)
+
+
+def test_size_queries(lib):
+    assert lib.zr_version() >= 100
+    assert lib.zr_spectrum_pitch(2048) == 1028
+    assert lib.zr_spectrum_elems(2048, 2048) == 2049 * 1028
+    assert lib.zr_xcorr_work_bytes(10, 2048, 100) == 10 * 200 * 1028 * 8
+
+
+def test_errors_are_reported_without_a_gpu(lib):
+    from zorro_gb300 import _lib
+    rc = lib.zr_locate_peaks(None, 1, 100, None, None, None)
+    assert rc == -1
+    assert "null" in _lib.last_error()
+
+
+@pytest.mark.parametrize("mode,w", [("tri", 5), ("diag", 3), ("diag", 1), ("first", 5), ("auto", 5)])
+def test_tri_indices_and_equation_matrix(mode, w):
+    for N in (2, 7, 40):
+        t = hm.tri_indices(N, mode, w, 0)
+        assert np.array_equal(t, zo.tri_indices(N, mode, w, 0))
+        if mode != "first" and N > 1:
+            r = t[:-1, 1:]
+            assert np.array_equal(hm.equation_matrix(r), zo.solver_matrix(r))
+
+
+def test_shift_kernels_match_reference_kernel():
+    rng = np.random.default_rng(0)
+    t = rng.normal(0, 3, size=(20, 2))
+    for (ry, rx, ap, ky, kx), tt in zip(hm.shift_params(t), t):
+        assert (ry, rx) == tuple(np.round(tt).astype(int))
+        k2 = zo.lanczos_kernel(np.remainder(tt, 1))
+        if ap:
+            np.testing.assert_allclose(np.outer(ky, kx), k2, rtol=1e-12, atol=1e-15)
+
+
+def test_frc_tiles_match_oracle():
+    rng = np.random.default_rng(1)
+    for shape in ((800, 800), (3838, 3710), (1024, 1024)):
+        t = rng.normal(0, 4, size=(10, 2))
+        t -= t.mean(axis=0)
+        offs, tiles = hm.frc_tiles(shape, t)
+        crop = zo.frc_crop_limits(t)
+        assert tiles[0] * tiles[1] == len(offs)
+        if len(offs):
+            assert offs[0, 0] == int(crop[0]) and offs[0, 1] == int(crop[1])
+
+
+def test_dose_constants_match_oracle():
+    dt = zo.Dtypes(True)
+    for P, ps, dose in (((1024, 1024), 0.1, 1.0), ((4096, 4096), 0.105, 1.2 * 1.05 ** 2)):
+        p = [dose, 0.24499, -1.6649, 2.8141, 32, 0]
+        a = hm.dose_constants(40, P, ps, 300.0, p)
+        b = zo.dose_filter_params(40, P, ps, 300.0, p, dt=dt)
+        np.testing.assert_allclose(a["thresQ"], b["thresQ"], rtol=1e-12)
+        np.testing.assert_allclose(a["dose_end"], b["accum"][1:], rtol=1e-12)
+
+
+def test_hotpix_fit_matches_oracle():
+    from zorro_gb300.synthetic import make_movie
+    mv = make_movie(20, (128, 120), seed=11, mean_dose=1.6, dtype="uint8", gain_map=True, hot_fraction=1e-3)
+    usum = np.sum(mv["images"], axis=0)
+    info = dict(zo.DEFAULTS["hotpixInfo"])
+    ref = zo.hotpix_fit(usum, info, 20, zo.Dtypes(True))
+    sm, ps, edges = hm.hotpix_bins(np.float64(np.sum(usum, dtype=np.float64)) / usum.size, info["maxSigma"])
+    hist, _ = np.histogram(usum, edges)
+    mu, sg, cl, cu, _ = hm.hotpix_fit(hist, edges, sm, ps, info)
+    assert mu == pytest.approx(ref["mu"], rel=1e-6)
+    assert sg == pytest.approx(ref["sigma"], rel=1e-6)
+    assert cl == ref["cutoffLower"] or (np.isnan(cl) and np.isnan(ref["cutoffLower"]))
+    assert cu == pytest.approx(float(ref["cutoffUpper"]), rel=1e-5)
+
+
+def test_numpy_axis0_sum_is_sequential():
+    """The hot-pixel kernel sums frames in order in float32, which is what
+    np.sum(stack, axis=0) does for a float32 stack."""
+    rng = np.random.default_rng(3)
+    a = (rng.random((40, 64, 64)) * 3).astype(np.float32)
+    s = np.zeros((64, 64), np.float32)
+    for k in range(40):
+        s = s + a[k]
+    assert np.array_equal(np.sum(a, axis=0), s)

@@ -1,0 +1,90 @@
+"""GPU kernels against the oracle, one stage at a time (through the C ABI)."""
+import numpy as np
+import pytest
+
+from oracle import zorro_oracle as zo
+from zorro_gb300.synthetic import make_movie
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small():
+    mv = make_movie(5, (100, 90), seed=2, mean_dose=3.0, drift_sigma=1.0)
+    return mv["images"]
+
+
+def crop_layout(F, P, C_):
+    """The kernels' spectrum layout from a full P0 x P1 spectrum."""
+    C0, C1 = C_
+    rows = [r if r < C0 // 2 else P[0] - C0 + r for r in range(C0)] + [C0 // 2]
+    return F[np.array(rows)][:, :C1 // 2 + 1]
+
+
+@pytest.mark.parametrize("P,C_", [((128, 128), (64, 64)), ((128, 256), (128, 128)), ((256, 256), (256, 256))])
+def test_spectra_match_numpy_fft(small, P, C_):
+    from tests import gpu_helpers as gh
+    G, S, GM, means, _ = gh.spectra(small, P, C_)
+    N, H, W = small.shape
+    np.testing.assert_allclose(means, small.reshape(N, -1).astype(np.float64).mean(axis=1), rtol=1e-5)
+    m = np.zeros(P)
+    m[:H, :W] = 1
+    gm_ref = crop_layout(np.fft.fft2(m), P, C_)
+    np.testing.assert_allclose(GM[:, :C_[1] // 2 + 1], gm_ref, atol=1e-4 * np.abs(gm_ref).max())
+    for n in range(N):
+        u = np.zeros(P)
+        u[:H, :W] = small[n].astype(np.float64) - means[n]
+        g_ref = crop_layout(np.fft.fft2(u), P, C_)
+        s_ref = crop_layout(np.fft.fft2(u * u), P, C_)
+        np.testing.assert_allclose(G[n][:, :C_[1] // 2 + 1], g_ref, atol=2e-6 * np.abs(g_ref).max() * np.sqrt(P[0] * P[1]) / 16)
+        np.testing.assert_allclose(S[n][:, :C_[1] // 2 + 1], s_ref, atol=2e-6 * np.abs(s_ref).max() * np.sqrt(P[0] * P[1]) / 16)
+
+
+@pytest.mark.parametrize("P,C_,mS", [((128, 128), (64, 64), 12), ((256, 256), (128, 128), 20)])
+def test_correlation_windows_match_oracle(small, P, C_, mS):
+    """C windows of mnxc2 (float32, mean-subtracted) vs the float64 oracle."""
+    from tests import gpu_helpers as gh
+    N = small.shape[0]
+    _, _, _, _, dev = gh.spectra(small, P, C_)
+    pairs = [(I, J) for I in range(N) for J in range(I + 1, N)]
+    _, cw, _ = gh.windows(dev, N, C_, mS, pairs)
+    dt = zo.Dtypes(True)
+    padded, mask = zo.pad_stack(small, P)
+    sC = np.array(C_)
+    GM, MP = zo.mask_spectrum(mask, sC, dt)
+    nc2 = zo.norm_const2(sC)
+    spec = [zo.frame_spectra(padded[n], mask, sC, dt) for n in range(N)]
+    for k, (I, J) in enumerate(pairs):
+        ref, _ = zo.mnxc2(spec[I][0], spec[I][1], spec[J][0], spec[J][1], GM, MP, nc2, mS, suppressOrigin=False, dt=dt)
+        scale = np.abs(ref).max()
+        err = np.abs(cw[k] - ref).max() / scale
+        assert err < 2e-5, (I, J, err)
+
+
+def test_peaks_match_oracle_on_same_windows(small):
+    """locatePeak on the GPU vs the oracle, fed the same (GPU) windows."""
+    from tests import gpu_helpers as gh
+    P, C_, mS = (256, 256), (128, 128), 20
+    N = small.shape[0]
+    _, _, _, _, dev = gh.spectra(small, P, C_)
+    pairs = [(I, J) for I in range(N) for J in range(I + 1, N)]
+    _, cw, cw_dev = gh.windows(dev, N, C_, mS, pairs)
+    res = gh.peaks(cw_dev, mS)
+    mmask = zo.max_shift_mask(mS)
+    dt = zo.Dtypes(True)
+    agree = 0
+    for k in range(len(pairs)):
+        C = cw[k].astype(np.float64).copy()
+        origin = C[mS, mS]
+        C0 = np.fft.ifftshift(C)  # back to FFT order for the suppressOrigin stencil
+        C0[0, 0] = 0.125 * (C0[1, 0] + C0[0, 1] + C0[-1, 0] + C0[-1, 0] + C0[1, 1] + C0[-1, 1] + C0[-1, 1] + C0[-1, -1])
+        C = np.fft.fftshift(C0)
+        r = zo.locate_peak(C, mmask, 16, "opti", dt=dt)
+        assert res["origin"][k] == pytest.approx(origin, rel=1e-6)
+        assert abs(res["sigma"][k] - r["sigma"]) < 0.02, (k, res["sigma"][k], r["sigma"])
+        assert res["peaksig"][k] == pytest.approx(r["peaksig"], rel=1e-3)
+        same = np.allclose([res["sy"][k], res["sx"][k]], r["shift"], atol=1e-9)
+        agree += same
+        if not same:
+            assert np.abs(np.array([res["sy"][k], res["sx"][k]]) - r["shift"]).max() <= 1.0 / 16 + 1e-9
+    assert agree >= len(pairs) - 1

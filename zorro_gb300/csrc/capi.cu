@@ -1,0 +1,90 @@
+// Library-wide C ABI pieces: error reporting, per-device initialisation and
+// the twiddle table.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+
+#include "common.cuh"
+#include "internal.h"
+
+#define ZR_VERSION 100
+
+namespace zr {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return ZR_OK;
+  return set_error(ZR_ECUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+static std::atomic<unsigned long long> g_launches{0};
+
+int launched(const char* what) {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cuda_check(cudaGetLastError(), what);
+}
+
+// W_8192^k = exp(-2 pi i k / 8192), one copy per device.
+static __device__ float2 d_twiddle[TWN];
+
+static std::mutex g_init_mu;
+static bool g_init_done[64];
+static const float2* g_tw_ptr[64];
+
+static int init_device(int dev) {
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if (dev < 0 || dev >= 64) return set_error(ZR_EINVAL, "device %d out of range", dev);
+  if (g_init_done[dev]) return ZR_OK;
+  int prev = 0;
+  ZR_TRY(cuda_check(cudaGetDevice(&prev), "cudaGetDevice"));
+  if (prev != dev) ZR_TRY(cuda_check(cudaSetDevice(dev), "cudaSetDevice"));
+  static float2 host[TWN];
+  for (int k = 0; k < TWN; k++) {
+    const double a = -2.0 * M_PI * (double)k / (double)TWN;
+    host[k] = make_float2((float)cos(a), (float)sin(a));
+  }
+  int rc = cuda_check(cudaMemcpyToSymbol(d_twiddle, host, sizeof(host)), "twiddle upload");
+  void* p = nullptr;
+  if (rc == ZR_OK) rc = cuda_check(cudaGetSymbolAddress(&p, d_twiddle), "twiddle address");
+  if (prev != dev) cudaSetDevice(prev);
+  if (rc != ZR_OK) return rc;
+  g_tw_ptr[dev] = (const float2*)p;
+  g_init_done[dev] = true;
+  return ZR_OK;
+}
+
+const float2* twiddles() {
+  int dev = 0;
+  if (cuda_check(cudaGetDevice(&dev), "cudaGetDevice") != ZR_OK) return nullptr;
+  if (dev < 0 || dev >= 64) return nullptr;
+  if (!g_init_done[dev] && init_device(dev) != ZR_OK) return nullptr;
+  return g_tw_ptr[dev];
+}
+
+}  // namespace zr
+
+extern "C" int zr_version(void) { return ZR_VERSION; }
+
+extern "C" int zr_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return (int)strlen(zr::g_err);
+  strncpy(buf, zr::g_err, len - 1);
+  buf[len - 1] = 0;
+  return (int)strlen(buf);
+}
+
+extern "C" int zr_init(int device) { return zr::init_device(device); }
+
+extern "C" unsigned long long zr_launch_count(void) { return zr::g_launches.load(); }

@@ -1,0 +1,64 @@
+// Shared device-side helpers for the Zorro movie-registration kernels.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/zorro_gb300.h"
+#include "fft_core.cuh"
+
+namespace zr {
+
+// One movie's frames as the kernels read them.  The corrected value of
+// pixel (y, x) of frame n is
+//     v = float32(gain[y,x] * raw[n,y,x])          (loadData, zorro.py:3466)
+//     v = v / gdiv                                  (zorro.py:3477-3478, if gdiv != 0)
+//     v = ha[y,x] * v + hb[y,x]                     (hotpixFilter, zorro.py:2649)
+// with each step skipped when its pointer (or gdiv) is null/zero.
+struct FrameSrc {
+  const void* raw;
+  int type;  // ZR_F32, ZR_U8, ZR_U16, ZR_F16
+  const float* gain;
+  const float* ha;
+  const float* hb;
+  float gdiv;
+  int N, H, W;
+  long long fstride;  // elements between consecutive frames
+};
+
+__host__ inline FrameSrc make_src(const zr_frames_t* f) {
+  FrameSrc s;
+  s.raw = f->raw;
+  s.type = f->raw_type;
+  s.gain = f->gain;
+  s.ha = f->hot_a;
+  s.hb = f->hot_b;
+  s.gdiv = f->gain_divisor;
+  s.N = f->n_frames;
+  s.H = f->height;
+  s.W = f->width;
+  s.fstride = f->frame_stride ? f->frame_stride : (long long)f->height * f->width;
+  return s;
+}
+
+__device__ __forceinline__ float load_raw(const FrameSrc& f, long long idx) {
+  switch (f.type) {
+    case ZR_U8: return (float)__ldg((const uint8_t*)f.raw + idx);
+    case ZR_U16: return (float)__ldg((const uint16_t*)f.raw + idx);
+    case ZR_F16: return __half2float(__ldg((const __half*)f.raw + idx));
+    default: return __ldg((const float*)f.raw + idx);
+  }
+}
+
+__device__ __forceinline__ float load_corrected(const FrameSrc& f, int n, int y, int x) {
+  const long long p = (long long)y * f.W + x;
+  float v = load_raw(f, (long long)n * f.fstride + p);
+  if (f.gain) v = __fmul_rn(__ldg(f.gain + p), v);
+  if (f.gdiv != 0.0f) v = __fdiv_rn(v, f.gdiv);
+  if (f.ha) v = __fmaf_rn(__ldg(f.ha + p), v, __ldg(f.hb + p));
+  return v;
+}
+
+__device__ __forceinline__ int ilog2c(int v) { return 31 - __clz(v); }
+
+}  // namespace zr

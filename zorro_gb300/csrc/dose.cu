@@ -1,0 +1,297 @@
+// Dose-weighted sum (doseFilter, zorro.py:2349-2494), the Unblur filter:
+//
+//   filtSum = | IFFT( sum_n FFT(pad_sym(frame_n)) * thres_n(q) * filt_n(q) ) |[:H, :W]
+//   filt_n(q)  = exp(-0.5 * dose_end_n / critDose(q)),
+//   critDose(q) = vs * (A q^B + C)   (the value at the Nyquist corner is
+//                 replaced by the square of its left neighbour, zorro.py:2422),
+//   thres_n(q) = exp(-(q / thresQ_n)^order).
+//
+// The filters are real and even in frequency, so the accumulated spectrum is
+// Hermitian: only kx in [0, P1/2] is kept.  Two aligned frames share one
+// complex row FFT; the column pass applies each frame's filter and
+// accumulates in shared memory; the inverse column pass keeps only the H
+// output rows and the final row pass packs two rows per complex inverse FFT.
+#include <math.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace zr {
+
+constexpr int DS_NBR = 4;  // rows per CTA (forward row pass)
+constexpr int DS_NBC = 2;  // columns per CTA (accumulating column pass)
+
+__device__ __forceinline__ int sym_idx(int i, int n) {
+  int m = i % (2 * n);
+  return m < n ? m : 2 * n - 1 - m;
+}
+
+template <int P1>
+__global__ void __launch_bounds__(fft_threads(P1, DS_NBR))
+    k_dose_rows(const float* __restrict__ img, int N, int H, int W, int f0, int K4, int P0,
+                float2* __restrict__ RW, const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(P1, DS_NBR);
+  constexpr int LD = ld_of(P1);
+  extern __shared__ float2 sm[];
+  const int g = blockIdx.x;
+  const int pl = blockIdx.y;              // frame pair within the chunk
+  const int na = f0 + 2 * pl, nb = na + 1;
+  for (int e = threadIdx.x; e < DS_NBR * P1; e += T) {
+    const int r = e / P1, x = e - r * P1;
+    const int ys = sym_idx(g * DS_NBR + r, H), xs = sym_idx(x, W);
+    const size_t p = (size_t)ys * W + xs;
+    const float a = img[(size_t)na * H * W + p];
+    const float b = nb < N ? img[(size_t)nb * H * W + p] : 0.0f;
+    sm[r * LD + pidx(x)] = make_float2(a, b);
+  }
+  __syncthreads();
+  block_fft<P1, DS_NBR, T, -1>(sm, tw);
+  const size_t H4 = P0 / DS_NBR;
+  const size_t fa = (size_t)(2 * pl) * H4 * K4 * DS_NBR;
+  const size_t fb = fa + H4 * K4 * DS_NBR;
+  const size_t base = (size_t)g * K4 * DS_NBR;
+  for (int e = threadIdx.x; e < K4 * DS_NBR; e += T) {
+    const int k = e / DS_NBR, r = e - k * DS_NBR;
+    float2 U = make_float2(0.0f, 0.0f), V = U;
+    if (k <= P1 / 2) {
+      const float2 zk = sm[r * LD + pidx(k)];
+      const float2 zm = sm[r * LD + pidx((P1 - k) & (P1 - 1))];
+      U = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      V = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    }
+    RW[fa + base + e] = U;
+    if (nb < N) RW[fb + base + e] = V;
+  }
+}
+
+__device__ __forceinline__ float crit_dose(const zr_dose_params_t& p, int fy, int fx) {
+  const float q = sqrtf((float)fx * (float)fx * (p.inv_ps_x * p.inv_ps_x) + (float)fy * (float)fy * (p.inv_ps_y * p.inv_ps_y));
+  return p.voltage_scaling * (p.crit_a * powf(q, p.crit_b) + p.crit_c);
+}
+
+__device__ __forceinline__ void dose_weight(const zr_dose_params_t& p, int P0, int P1, int ky, int kx, float dose_end,
+                                            float tq, float& w) {
+  const int fy = ky < P0 / 2 ? ky : ky - P0;
+  const int fx = kx;
+  const float q = sqrtf((float)fx * (float)fx * (p.inv_ps_x * p.inv_ps_x) + (float)fy * (float)fy * (p.inv_ps_y * p.inv_ps_y));
+  float crit;
+  if (ky == P0 / 2 && kx == P1 / 2) {
+    const float c = crit_dose(p, fy, P1 / 2 - 1);
+    crit = c * c;
+  } else {
+    crit = p.voltage_scaling * (p.crit_a * powf(q, p.crit_b) + p.crit_c);
+  }
+  const float filt = expf((-0.5f * dose_end) / crit);
+  const float thres = expf(-powf(q / tq, p.cutoff_order));
+  w = thres * filt;
+}
+
+template <int P0>
+__global__ void __launch_bounds__(fft_threads(P0, DS_NBC))
+    k_dose_cols(const float2* __restrict__ RW, int f0, int nfr, int K4, int P1, zr_dose_params_t prm,
+                const float* __restrict__ thres_q, const float* __restrict__ dose_end, int first,
+                float2* __restrict__ ACC, float* __restrict__ FM, const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(P0, DS_NBC);
+  constexpr int LD = ld_of(P0);
+  constexpr int H4 = P0 / DS_NBR;
+  extern __shared__ float2 sm[];
+  float2* acc = sm + DS_NBC * LD;                  // [DS_NBC][P0]
+  float* fm = (float*)(acc + DS_NBC * P0);          // [DS_NBC][P0]
+  const int k0 = blockIdx.x * DS_NBC;
+  for (int e = threadIdx.x; e < DS_NBC * P0; e += T) {
+    const int c = e / P0, y = e - c * P0;
+    acc[e] = first ? make_float2(0.0f, 0.0f) : ACC[(size_t)y * K4 + k0 + c];
+    fm[e] = (first || !prm.normalize) ? 0.0f : FM[(size_t)y * K4 + k0 + c];
+  }
+  for (int nl = 0; nl < nfr; nl++) {
+    const float2* R = RW + (size_t)nl * H4 * K4 * DS_NBR;
+    __syncthreads();
+    for (int e = threadIdx.x; e < H4 * DS_NBC * DS_NBR; e += T) {
+      const int gg = e / (DS_NBC * DS_NBR), j = e - gg * (DS_NBC * DS_NBR);
+      const int c = j / DS_NBR, r = j - c * DS_NBR;
+      sm[c * LD + pidx(gg * DS_NBR + r)] = R[((size_t)gg * K4 + k0) * DS_NBR + j];
+    }
+    __syncthreads();
+    block_fft<P0, DS_NBC, T, -1>(sm, tw);
+    const float de = dose_end[f0 + nl], tq = thres_q[f0 + nl];
+    for (int e = threadIdx.x; e < DS_NBC * P0; e += T) {
+      const int c = e / P0, y = e - c * P0;
+      const int kx = k0 + c;
+      if (kx > P1 / 2) continue;
+      float w;
+      dose_weight(prm, P0, P1, y, kx, de, tq, w);
+      const float2 F = sm[c * LD + pidx(y)];
+      acc[e] = make_float2(acc[e].x + F.x * w, acc[e].y + F.y * w);
+      if (prm.normalize) fm[e] += w;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < DS_NBC * P0; e += T) {
+    const int c = e / P0, y = e - c * P0;
+    ACC[(size_t)y * K4 + k0 + c] = acc[e];
+    if (prm.normalize) FM[(size_t)y * K4 + k0 + c] = fm[e];
+  }
+}
+
+// Inverse column pass, keeping rows [0, H).
+template <int P0>
+__global__ void __launch_bounds__(fft_threads(P0, DS_NBR))
+    k_dose_icols(const float2* __restrict__ ACC, const float* __restrict__ FM, int normalize, int K4, int H,
+                 float2* __restrict__ T2, const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(P0, DS_NBR);
+  constexpr int LD = ld_of(P0);
+  extern __shared__ float2 sm[];
+  const int k0 = blockIdx.x * DS_NBR;
+  for (int e = threadIdx.x; e < DS_NBR * P0; e += T) {
+    const int y = e / DS_NBR, c = e - y * DS_NBR;
+    float2 v = ACC[(size_t)y * K4 + k0 + c];
+    if (normalize) {
+      const float s = 1.0f / (FM[(size_t)y * K4 + k0 + c] + 1.0f);
+      v = make_float2(v.x * s, v.y * s);
+    }
+    sm[c * LD + pidx(y)] = v;
+  }
+  __syncthreads();
+  block_fft<P0, DS_NBR, T, 1>(sm, tw);
+  for (int e = threadIdx.x; e < H * DS_NBR; e += T) {
+    const int y = e / DS_NBR, c = e - y * DS_NBR;
+    T2[(size_t)y * K4 + k0 + c] = sm[c * LD + pidx(y)];
+  }
+}
+
+// Real-output inverse row pass (two rows per complex FFT), |.|, crop, scale.
+template <int P1>
+__global__ void __launch_bounds__(fft_threads(P1, 2))
+    k_dose_irows(const float2* __restrict__ T2, int K4, int H, int W, float scale, float* __restrict__ out,
+                 const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(P1, 2);
+  constexpr int LD = ld_of(P1);
+  constexpr int half = P1 / 2;
+  extern __shared__ float2 sm[];
+  const int y0 = blockIdx.x * 4;
+  for (int e = threadIdx.x; e < 2 * (half + 1); e += T) {
+    const int p = e / (half + 1), k = e - p * (half + 1);
+    const int a0 = y0 + 2 * p, a1 = a0 + 1;
+    const float2 ga = a0 < H ? T2[(size_t)a0 * K4 + k] : make_float2(0.0f, 0.0f);
+    const float2 gb = a1 < H ? T2[(size_t)a1 * K4 + k] : make_float2(0.0f, 0.0f);
+    float2* s = sm + p * LD;
+    if (k == 0 || k == half) {
+      s[pidx(k)] = make_float2(ga.x, gb.x);
+    } else {
+      s[pidx(k)] = make_float2(ga.x - gb.y, ga.y + gb.x);
+      s[pidx(P1 - k)] = make_float2(ga.x + gb.y, -ga.y + gb.x);
+    }
+  }
+  __syncthreads();
+  block_fft<P1, 2, T, 1>(sm, tw);
+  for (int e = threadIdx.x; e < 4 * W; e += T) {
+    const int q = e / W, x = e - q * W;
+    const int y = y0 + q;
+    if (y >= H) continue;
+    const float2 v = sm[(q >> 1) * LD + pidx(x)];
+    out[(size_t)y * W + x] = fabsf(((q & 1) ? v.y : v.x) * scale);
+  }
+}
+
+template <int P>
+static int set_smem(const void* fn, size_t smem) {
+  return cuda_check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "dose attr");
+}
+
+#define ZR_DOSE_DISPATCH(L, CALL)                               \
+  switch (L) {                                                  \
+    case 256: { constexpr int LL = 256; CALL; } break;          \
+    case 512: { constexpr int LL = 512; CALL; } break;          \
+    case 1024: { constexpr int LL = 1024; CALL; } break;        \
+    case 2048: { constexpr int LL = 2048; CALL; } break;        \
+    case 4096: { constexpr int LL = 4096; CALL; } break;        \
+    default: return set_error(ZR_ESIZE, "dose filter size %d not supported", (int)(L)); \
+  }
+
+template <int P1>
+static int dose_rows(const float* img, int N, int H, int W, int f0, int npairs, int K4, int P0, float2* RW,
+                     const float2* tw, cudaStream_t st) {
+  const size_t smem = (size_t)DS_NBR * ld_of(P1) * sizeof(float2);
+  ZR_TRY(set_smem<P1>((const void*)k_dose_rows<P1>, smem));
+  k_dose_rows<P1><<<dim3(P0 / DS_NBR, npairs), fft_threads(P1, DS_NBR), smem, st>>>(img, N, H, W, f0, K4, P0, RW, tw);
+  return launched("k_dose_rows");
+}
+
+template <int P0>
+static int dose_cols(const float2* RW, int f0, int nfr, int K4, int P1, const zr_dose_params_t& prm,
+                     const float* tq, const float* de, int first, float2* ACC, float* FM, const float2* tw,
+                     cudaStream_t st) {
+  const size_t smem = (size_t)DS_NBC * ld_of(P0) * sizeof(float2) + (size_t)DS_NBC * P0 * (sizeof(float2) + sizeof(float));
+  ZR_TRY(set_smem<P0>((const void*)k_dose_cols<P0>, smem));
+  k_dose_cols<P0><<<K4 / DS_NBC, fft_threads(P0, DS_NBC), smem, st>>>(RW, f0, nfr, K4, P1, prm, tq, de, first, ACC,
+                                                                       FM, tw);
+  return launched("k_dose_cols");
+}
+
+template <int P0>
+static int dose_icols(const float2* ACC, const float* FM, int normalize, int K4, int H, float2* T2, const float2* tw,
+                      cudaStream_t st) {
+  const size_t smem = (size_t)DS_NBR * ld_of(P0) * sizeof(float2);
+  ZR_TRY(set_smem<P0>((const void*)k_dose_icols<P0>, smem));
+  k_dose_icols<P0><<<K4 / DS_NBR, fft_threads(P0, DS_NBR), smem, st>>>(ACC, FM, normalize, K4, H, T2, tw);
+  return launched("k_dose_icols");
+}
+
+template <int P1>
+static int dose_irows(const float2* T2, int K4, int H, int W, float scale, float* out, const float2* tw,
+                      cudaStream_t st) {
+  const size_t smem = (size_t)2 * ld_of(P1) * sizeof(float2);
+  ZR_TRY(set_smem<P1>((const void*)k_dose_irows<P1>, smem));
+  k_dose_irows<P1><<<(H + 3) / 4, fft_threads(P1, 2), smem, st>>>(T2, K4, H, W, scale, out, tw);
+  return launched("k_dose_irows");
+}
+
+}  // namespace zr
+
+using namespace zr;
+
+static size_t dose_fixed_bytes(int P0, int P1) {
+  const size_t K4 = zr_spectrum_pitch(P1);
+  return (size_t)P0 * K4 * (2 * sizeof(float2) + sizeof(float));
+}
+
+static size_t dose_frame_bytes(int P0, int P1) { return (size_t)P0 * zr_spectrum_pitch(P1) * sizeof(float2); }
+
+extern "C" size_t zr_dose_work_bytes(int P0, int P1, int n_frames) {
+  return dose_fixed_bytes(P0, P1) + (size_t)n_frames * dose_frame_bytes(P0, P1);
+}
+
+extern "C" int zr_dose_filter(const float* aligned, int N, int H, int W, const zr_dose_params_t* params,
+                              const float* thres_q, const float* dose_end, int P0, int P1, float* filt_sum,
+                              void* work, size_t work_bytes, void* stream) {
+  if (!aligned || !params || !thres_q || !dose_end || !filt_sum || !work)
+    return set_error(ZR_EINVAL, "zr_dose_filter: null argument");
+  if (N <= 0 || H <= 0 || W <= 0 || H > P0 || W > P1) return set_error(ZR_EINVAL, "zr_dose_filter: bad sizes");
+  if (!is_pow2(P0) || !is_pow2(P1) || P0 < 256 || P1 < 256 || P0 > 4096 || P1 > 4096)
+    return set_error(ZR_ESIZE, "zr_dose_filter: padded size %dx%d must be a power of two in [256, 4096]", P0, P1);
+  const size_t fixed = dose_fixed_bytes(P0, P1), per = dose_frame_bytes(P0, P1);
+  if (work_bytes < fixed + 2 * per)
+    return set_error(ZR_EWORK, "zr_dose_filter: work buffer %zu < %zu", work_bytes, fixed + 2 * per);
+  int chunk = (int)((work_bytes - fixed) / per);
+  chunk &= ~1;
+  if (chunk > N + (N & 1)) chunk = N + (N & 1);
+  const float2* tw = twiddles();
+  if (!tw) return ZR_ECUDA;
+  const int K4 = zr_spectrum_pitch(P1);
+  float2* ACC = (float2*)work;
+  float2* T2 = ACC + (size_t)P0 * K4;
+  float* FM = (float*)(T2 + (size_t)P0 * K4);
+  float2* RW = (float2*)(FM + (size_t)P0 * K4);
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int f0 = 0; f0 < N; f0 += chunk) {
+    const int nfr = (N - f0) < chunk ? (N - f0) : chunk;
+    const int npairs = (nfr + 1) / 2;
+    ZR_DOSE_DISPATCH(P1, ZR_TRY((dose_rows<LL>(aligned, N, H, W, f0, npairs, K4, P0, RW, tw, st))));
+    ZR_DOSE_DISPATCH(P0, ZR_TRY((dose_cols<LL>(RW, f0, nfr, K4, P1, *params, thres_q, dose_end, f0 == 0, ACC, FM,
+                                                tw, st))));
+  }
+  ZR_DOSE_DISPATCH(P0, ZR_TRY((dose_icols<LL>(ACC, FM, params->normalize, K4, H, T2, tw, st))));
+  const float scale = (float)(1.0 / ((double)P0 * P1));
+  ZR_DOSE_DISPATCH(P1, ZR_TRY((dose_irows<LL>(T2, K4, H, W, scale, filt_sum, tw, st))));
+  return ZR_OK;
+}

@@ -1,0 +1,34 @@
+// Internal helpers shared by the translation units of libzorrogb.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace zr {
+
+// Record an error message for zr_last_error() and return ``code``.
+int set_error(int code, const char* fmt, ...);
+// Check a CUDA runtime result; on failure record it and return ZR_ECUDA.
+int cuda_check(cudaError_t e, const char* what);
+// Count one kernel launch and check it was accepted.
+int launched(const char* what);
+// Twiddle table of the current device (initialises it on first use).
+const float2* twiddles();
+
+inline bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
+inline int ilog2(long long v) {
+  int l = 0;
+  while ((1LL << l) < v) ++l;
+  return l;
+}
+
+// Threads for a batched shared-memory FFT of NB sequences of length L.
+constexpr int fft_threads(int L, int NB) {
+  return (NB * L / 32 < 64) ? 64 : ((NB * L / 32 > 512) ? 512 : NB * L / 32);
+}
+
+}  // namespace zr
+
+#define ZR_TRY(expr)            \
+  do {                          \
+    int _zr_rc = (expr);        \
+    if (_zr_rc != 0) return _zr_rc; \
+  } while (0)

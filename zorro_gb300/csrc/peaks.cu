@@ -1,0 +1,473 @@
+// Peak search on the correlation windows (locatePeak, zorro.py:1099-1231).
+//
+// One CTA per pair keeps the w x w window in shared memory and runs, with all
+// threads in lock step:
+//   * suppressOrigin (zorro.py:1078-1083, literal stencil);
+//   * Bmode 'opti': a bounded Brent minimisation over sigma in [0, 7] of
+//     std(G_sigma*C) / (max - mean) (zorro.py:1108-1121).  The minimiser is
+//     Brent's golden-section/parabolic method as published by Forsythe,
+//     Malcolm and Moler (FMIN, 1977), the method behind scipy's
+//     minimize_scalar(method='bounded'); each function value is a full
+//     separable Gaussian filter of the window with 'reflect' borders and
+//     radius int(4 sigma + 0.5), the filter scipy.ndimage.gaussian_filter
+//     applies (axis 0, then axis 1);
+//   * the maxShift circular mask, the argmax (first index on ties) and the
+//     peak significance (zorro.py:1165-1168);
+//   * the sub-pixel step: the 16 x 16 patch around the peak, its DFT,
+//     zero-padded to 16*subPixReg and inverted, |.| and its argmax
+//     (zorro.py:1180-1216), or the integer fallback at the window edge.
+// Filtered values are recomputed on the fly in blocks of rows, so the CTA
+// needs only the window and one row block of shared memory.
+#include <math.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace zr {
+
+constexpr int PK_T = 512;
+constexpr int PK_RB = 8;       // rows per vertical-filter block
+constexpr int PK_MAXR = 64;    // largest filter radius
+constexpr int PK_SUBR = 8;     // +/- patch half-size (zorro.py:619)
+
+struct PkShared {
+  float wy[2 * PK_MAXR + 1];
+  float wx[2 * PK_MAXR + 1];
+  double red[PK_T / 32][3];
+  float redf[PK_T / 32];
+  int redi[PK_T / 32];
+  double bc[4];
+  int bi[2];
+};
+
+__device__ __forceinline__ int reflect_idx(int i, int n) {
+  while (i < 0 || i >= n) {
+    if (i < 0) i = -i - 1;
+    if (i >= n) i = 2 * n - i - 1;
+  }
+  return i;
+}
+
+// Gaussian weights exp(-0.5 k^2 / sigma^2), normalised (double, then float).
+__device__ int gauss_weights(double sigma, float* w) {
+  if (!(sigma > 1e-15)) {
+    if (threadIdx.x == 0) w[0] = 1.0f;
+    return 0;
+  }
+  int r = (int)(4.0 * sigma + 0.5);
+  if (r > PK_MAXR) r = PK_MAXR;
+  if (threadIdx.x == 0) {
+    const double c = -0.5 / (sigma * sigma);
+    double s = 0.0;
+    double tmp[2 * PK_MAXR + 1];
+    for (int k = -r; k <= r; k++) {
+      tmp[k + r] = exp(c * (double)k * (double)k);
+      s += tmp[k + r];
+    }
+    for (int k = 0; k <= 2 * r; k++) w[k] = (float)(tmp[k] / s);
+  }
+  return r;
+}
+
+// Block reductions (all threads must call).
+__device__ double3 block_sum3(PkShared& sh, double a, double b, double c) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    c += __shfl_down_sync(0xffffffffu, c, o);
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { sh.red[wid][0] = a; sh.red[wid][1] = b; sh.red[wid][2] = c; }
+  __syncthreads();
+  if (wid == 0) {
+    a = lane < PK_T / 32 ? sh.red[lane][0] : 0.0;
+    b = lane < PK_T / 32 ? sh.red[lane][1] : 0.0;
+    c = lane < PK_T / 32 ? sh.red[lane][2] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if (lane == 0) { sh.bc[0] = a; sh.bc[1] = b; sh.bc[2] = c; }
+  }
+  __syncthreads();
+  double3 r = make_double3(sh.bc[0], sh.bc[1], sh.bc[2]);
+  __syncthreads();
+  return r;
+}
+
+// max value with the smallest index among equal values
+__device__ void block_argmax(PkShared& sh, float& v, int& idx) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_down_sync(0xffffffffu, v, o);
+    const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { sh.redf[wid] = v; sh.redi[wid] = idx; }
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < PK_T / 32 ? sh.redf[lane] : -INFINITY;
+    idx = lane < PK_T / 32 ? sh.redi[lane] : 0x7fffffff;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_down_sync(0xffffffffu, v, o);
+      const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+      if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+    if (lane == 0) { sh.bc[3] = v; sh.bi[0] = idx; }
+  }
+  __syncthreads();
+  v = (float)sh.bc[3];
+  idx = sh.bi[0];
+  __syncthreads();
+}
+
+struct FiltStats {
+  double s1, s2;   // sum (f - c), sum (f - c)^2
+  float mx;        // max f
+  int n;
+};
+
+// Visit every filtered value of the window.  MODE 0: statistics of all
+// values.  MODE 1: masked statistics plus argmax of (mask ? f : 0).
+template <int MODE>
+__device__ void filter_pass(const float* C, float* V, int w, int mS, int ry, int rx, const float* wy,
+                            const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st,
+                            float& amax, int& aidx) {
+  float s1 = 0.0f, s2 = 0.0f, mx = -INFINITY;
+  float bv = -INFINITY;
+  int bi = 0x7fffffff;
+  int cnt = 0;
+  for (int y0 = 0; y0 < w; y0 += PK_RB) {
+    const int nr = (w - y0) < PK_RB ? (w - y0) : PK_RB;
+    for (int e = threadIdx.x; e < nr * w; e += PK_T) {
+      const int i = e / w, x = e - i * w;
+      const int y = y0 + i;
+      float acc = 0.0f;
+      if (ry == 0) {
+        acc = C[y * w + x];
+      } else {
+        for (int k = -ry; k <= ry; k++) acc = fmaf(wy[k + ry], C[reflect_idx(y + k, w) * w + x], acc);
+      }
+      V[i * w + x] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * w; e += PK_T) {
+      const int i = e / w, x = e - i * w;
+      float f = 0.0f;
+      if (rx == 0) {
+        f = V[i * w + x];
+      } else {
+        for (int k = -rx; k <= rx; k++) f = fmaf(wx[k + rx], V[i * w + reflect_idx(x + k, w)], f);
+      }
+      const int y = y0 + i;
+      bool in = true;
+      if (MODE == 1) {
+        const int dy = y - mS, dx = x - mS;
+        in = !use_mask || (dy * dy + dx * dx < mS * mS);
+        const float mv = in ? f : 0.0f;
+        const int idx = y * w + x;
+        if (mv > bv || (mv == bv && idx < bi)) { bv = mv; bi = idx; }
+      }
+      if (in) {
+        const float d = f - c;
+        s1 += d;
+        s2 = fmaf(d, d, s2);
+        mx = fmaxf(mx, f);
+        cnt++;
+      }
+    }
+    __syncthreads();
+  }
+  double3 r = block_sum3(sh, (double)s1, (double)s2, (double)cnt);
+  st.s1 = r.x;
+  st.s2 = r.y;
+  st.n = (int)r.z;
+  float m = mx;
+  int dummy = 0;
+  block_argmax(sh, m, dummy);
+  st.mx = m;
+  if (MODE == 1) {
+    block_argmax(sh, bv, bi);
+    amax = bv;
+    aidx = bi;
+  }
+}
+
+__device__ double objective(const float* C, float* V, int w, int mS, double sigma, float c, PkShared& sh) {
+  const int r = gauss_weights(sigma, sh.wy);
+  __syncthreads();
+  FiltStats st;
+  float am;
+  int ai;
+  filter_pass<0>(C, V, w, mS, r, r, sh.wy, sh.wy, c, sh, false, st, am, ai);
+  const double n = (double)st.n;
+  const double m1 = st.s1 / n;
+  const double var = st.s2 / n - m1 * m1;
+  const double mean = (double)c + m1;
+  return sqrt(var > 0.0 ? var : 0.0) / ((double)st.mx - mean);
+}
+
+__device__ __forceinline__ double sgn1(double v) { return v > 0.0 ? 1.0 : (v < 0.0 ? -1.0 : 1.0); }
+
+// Bounded Brent minimisation (FMM FMIN).  Returns the abscissa of the best
+// value; *nfev receives the number of function values.
+__device__ double fmin_bounded(const float* C, float* V, int w, int mS, float c, PkShared& sh, double lo,
+                               double hi, double xatol, int maxfun, int* nfev) {
+  const double sqrt_eps = sqrt(2.2e-16);
+  const double golden = 0.5 * (3.0 - sqrt(5.0));
+  double a = lo, b = hi;
+  double fulc = a + golden * (b - a);
+  double nfc = fulc, xf = fulc;
+  double rat = 0.0, e = 0.0;
+  double x = xf;
+  double fx = objective(C, V, w, mS, x, c, sh);
+  int num = 1;
+  double ffulc = fx, fnfc = fx;
+  double xm = 0.5 * (a + b);
+  double tol1 = sqrt_eps * fabs(xf) + xatol / 3.0;
+  double tol2 = 2.0 * tol1;
+  while (fabs(xf - xm) > (tol2 - 0.5 * (b - a))) {
+    bool gstep = true;
+    if (fabs(e) > tol1) {
+      gstep = false;
+      double r = (xf - nfc) * (fx - ffulc);
+      double q = (xf - fulc) * (fx - fnfc);
+      double p = (xf - fulc) * q - (xf - nfc) * r;
+      q = 2.0 * (q - r);
+      if (q > 0.0) p = -p;
+      q = fabs(q);
+      r = e;
+      e = rat;
+      if ((fabs(p) < fabs(0.5 * q * r)) && (p > q * (a - xf)) && (p < q * (b - xf))) {
+        rat = (p + 0.0) / q;
+        x = xf + rat;
+        if (((x - a) < tol2) || ((b - x) < tol2)) rat = tol1 * sgn1(xm - xf);
+      } else {
+        gstep = true;
+      }
+    }
+    if (gstep) {
+      e = (xf >= xm) ? (a - xf) : (b - xf);
+      rat = golden * e;
+    }
+    x = xf + sgn1(rat) * fmax(fabs(rat), tol1);
+    const double fu = objective(C, V, w, mS, x, c, sh);
+    num += 1;
+    if (fu <= fx) {
+      if (x >= xf) a = xf; else b = xf;
+      fulc = nfc; ffulc = fnfc;
+      nfc = xf; fnfc = fx;
+      xf = x; fx = fu;
+    } else {
+      if (x < xf) a = x; else b = x;
+      if ((fu <= fnfc) || (nfc == xf)) {
+        fulc = nfc; ffulc = fnfc;
+        nfc = x; fnfc = fu;
+      } else if ((fu <= ffulc) || (fulc == xf) || (fulc == nfc)) {
+        fulc = x; ffulc = fu;
+      }
+    }
+    xm = 0.5 * (a + b);
+    tol1 = sqrt_eps * fabs(xf) + xatol / 3.0;
+    tol2 = 2.0 * tol1;
+    if (num >= maxfun) break;
+  }
+  *nfev = num;
+  return xf;
+}
+
+// Filtered value of the window at (y, x) (used for the 16 x 16 patch).
+__device__ float filtered_at(const float* C, int w, int y, int x, int ry, int rx, const float* wy, const float* wx) {
+  float f = 0.0f;
+  for (int kx = -rx; kx <= rx; kx++) {
+    const int xx = reflect_idx(x + kx, w);
+    float acc = 0.0f;
+    if (ry == 0) acc = C[y * w + xx];
+    else
+      for (int ky = -ry; ky <= ry; ky++) acc = fmaf(wy[ky + ry], C[reflect_idx(y + ky, w) * w + xx], acc);
+    f = (rx == 0) ? acc : fmaf(wx[kx + rx], acc, f);
+  }
+  return f;
+}
+
+__global__ void __launch_bounds__(PK_T) k_peaks(const float* __restrict__ cwin, int mS, zr_peak_params_t p,
+                                               zr_peak_result_t* __restrict__ res, const float2* __restrict__ tw) {
+  extern __shared__ float smf[];
+  __shared__ PkShared sh;
+  __shared__ float2 patchF[16 * 16];
+  const int w = 2 * mS;
+  const int w2 = w * w;
+  float* C = smf;
+  float* V = smf + w2;
+  const float* src = cwin + (size_t)blockIdx.x * w2;
+  for (int e = threadIdx.x; e < w2; e += PK_T) C[e] = src[e];
+  __syncthreads();
+  const float origin = C[mS * w + mS];
+  if (p.suppress_origin) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int o = mS * w + mS;
+      float s = C[o + w] + C[o + 1];
+      s = s + C[o - w];
+      s = s + C[o - w];
+      s = s + C[o + w + 1];
+      s = s + C[o - w + 1];
+      s = s + C[o - w + 1];
+      s = s + C[o - w - 1];
+      C[o] = 0.125f * s;
+    }
+    __syncthreads();
+  }
+  // mean of the window: the centring constant of the one-pass variances
+  float ls = 0.0f;
+  for (int e = threadIdx.x; e < w2; e += PK_T) ls += C[e];
+  double3 tot = block_sum3(sh, (double)ls, 0.0, 0.0);
+  const float c = (float)(tot.x / (double)w2);
+
+  double sigy = 0.0, sigx = 0.0, sig_opt = nan("");
+  int nfev = 0;
+  if (p.bmode == 1) {
+    sig_opt = fmin_bounded(C, V, w, mS, c, sh, p.opti_lo, p.opti_hi, p.opti_xatol, p.opti_maxiter, &nfev);
+    sigy = sigx = sig_opt;
+  } else if (p.bmode == 2) {
+    sigy = p.conv_sigma_y;
+    sigx = p.conv_sigma_x;
+  }
+  const int ry = gauss_weights(sigy, sh.wy);
+  const int rx = gauss_weights(sigx, sh.wx);
+  __syncthreads();
+  FiltStats st;
+  float amax = 0.0f;
+  int aidx = 0;
+  filter_pass<1>(C, V, w, mS, ry, rx, sh.wy, sh.wx, c, sh, p.use_mask != 0, st, amax, aidx);
+  const int cy = aidx / w, cx = aidx - (aidx / w) * w;
+  double peaksig = nan("");
+  {
+    const double n = (double)st.n;
+    const double m1 = st.s1 / n;
+    const double var = st.s2 / n - m1 * m1;
+    const double mean = (double)c + m1;
+    peaksig = ((double)amax - mean) / sqrt(var > 0.0 ? var : 0.0);
+  }
+  const float cval = C[cy * w + cx];
+  double shy = (double)cy - w / 2.0, shx = (double)cx - w / 2.0;
+  float corr = cval;
+  int flags = 0;
+  const int sp = p.sub_pix_reg;
+  if (sp > 1) {
+    if (cy - PK_SUBR >= 0 && cy + PK_SUBR <= w && cx - PK_SUBR >= 0 && cx + PK_SUBR <= w) {
+      // 16 x 16 filtered patch, then its forward DFT
+      __shared__ float patch[16 * 16];
+      for (int e = threadIdx.x; e < 256; e += PK_T) {
+        const int i = e >> 4, j = e & 15;
+        patch[e] = filtered_at(C, w, cy - PK_SUBR + i, cx - PK_SUBR + j, ry, rx, sh.wy, sh.wx);
+      }
+      __syncthreads();
+      // row DFTs then column DFTs (16-point, twiddles from the 8192 table)
+      __shared__ float2 rowF[16 * 16];
+      for (int e = threadIdx.x; e < 256; e += PK_T) {
+        const int i = e >> 4, v = e & 15;
+        float2 acc = make_float2(0.0f, 0.0f);
+        for (int j = 0; j < 16; j++) {
+          const float2 t = __ldg(tw + ((v * j) & 15) * (TWN / 16));
+          acc.x = fmaf(patch[i * 16 + j], t.x, acc.x);
+          acc.y = fmaf(patch[i * 16 + j], t.y, acc.y);
+        }
+        rowF[e] = acc;
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < 256; e += PK_T) {
+        const int u = e >> 4, v = e & 15;
+        float2 acc = make_float2(0.0f, 0.0f);
+        for (int i = 0; i < 16; i++) acc = cadd(acc, cmul(rowF[i * 16 + v], __ldg(tw + ((u * i) & 15) * (TWN / 16))));
+        patchF[e] = acc;
+      }
+      __syncthreads();
+      // Upsampled inverse DFT on an L x L grid, L = 16*sp: frequencies -8..7.
+      const int L = 16 * sp;
+      const int tws = TWN / L;
+      float2* Tx = (float2*)C;  // the window is no longer needed
+      __syncthreads();
+      for (int e = threadIdx.x; e < 16 * L; e += PK_T) {
+        const int fyi = e / L, nx = e - fyi * L;
+        float2 acc = make_float2(0.0f, 0.0f);
+        for (int fxi = 0; fxi < 16; fxi++) {
+          const int fx = fxi - 8;
+          const int m = ((fx * nx) % L + L) % L;
+          float2 t = __ldg(tw + m * tws);
+          t.y = -t.y;  // exp(+2 pi i m / L)
+          acc = cadd(acc, cmul(patchF[((fyi - 8) & 15) * 16 + (fx & 15)], t));
+        }
+        Tx[fyi * L + nx] = acc;
+      }
+      __syncthreads();
+      const float invL2 = 1.0f / ((float)L * (float)L);
+      float bv = -INFINITY;
+      int bi = 0x7fffffff;
+      for (int e = threadIdx.x; e < L * L; e += PK_T) {
+        const int ny = e / L, nx = e - ny * L;
+        float2 acc = make_float2(0.0f, 0.0f);
+        for (int fyi = 0; fyi < 16; fyi++) {
+          const int fy = fyi - 8;
+          const int m = ((fy * ny) % L + L) % L;
+          float2 t = __ldg(tw + m * tws);
+          t.y = -t.y;
+          acc = cadd(acc, cmul(Tx[fyi * L + nx], t));
+        }
+        const float mag = sqrtf(acc.x * acc.x + acc.y * acc.y) * invL2;
+        if (mag > bv || (mag == bv && e < bi)) { bv = mag; bi = e; }
+      }
+      block_argmax(sh, bv, bi);
+      const int sy = bi / L, sx = bi - (bi / L) * L;
+      const double ry0 = (double)cy - w / 2.0, rx0 = (double)cx - w / 2.0;
+      shy = ry0 + ((double)sy - L / 2.0 + (ry0 > 0 ? 1.0 : (ry0 < 0 ? -1.0 : 0.0))) / sp;
+      shx = rx0 + ((double)sx - L / 2.0 + (rx0 > 0 ? 1.0 : (rx0 < 0 ? -1.0 : 0.0))) / sp;
+      corr = (float)((double)bv / 256.0);
+    } else {
+      flags |= 1;
+    }
+  }
+  if (threadIdx.x == 0) {
+    zr_peak_result_t r;
+    r.shift_y = shy;
+    r.shift_x = shx;
+    r.sigma = sig_opt;
+    r.corr = corr;
+    r.peaksig = (float)peaksig;
+    r.origin = origin;
+    r.cy = cy;
+    r.cx = cx;
+    r.flags = flags;
+    r.nfev = nfev;
+    res[blockIdx.x] = r;
+  }
+}
+
+}  // namespace zr
+
+using namespace zr;
+
+extern "C" int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr_peak_params_t* params,
+                               zr_peak_result_t* results, void* stream) {
+  if (!cwin || !params || !results) return set_error(ZR_EINVAL, "zr_locate_peaks: null argument");
+  if (M <= 0) return ZR_OK;
+  const int w = 2 * max_shift;
+  if (max_shift < 8 || max_shift > 112)
+    return set_error(ZR_ESIZE, "zr_locate_peaks: maxShift %d outside [8, 112]", max_shift);
+  if (params->sub_pix_reg > 1 && (TWN % (16 * params->sub_pix_reg) != 0 || 16 * params->sub_pix_reg > 512))
+    return set_error(ZR_ESIZE, "zr_locate_peaks: subPixReg %d must be a power of two <= 32", params->sub_pix_reg);
+  if (params->bmode == 2 && (4.0 * params->conv_sigma_y + 0.5 > PK_MAXR || 4.0 * params->conv_sigma_x + 0.5 > PK_MAXR))
+    return set_error(ZR_ESIZE, "zr_locate_peaks: conv sigma too large");
+  if (params->bmode == 1 && 4.0 * params->opti_hi + 0.5 > PK_MAXR)
+    return set_error(ZR_ESIZE, "zr_locate_peaks: opti sigma bound too large");
+  const float2* tw = twiddles();
+  if (!tw) return ZR_ECUDA;
+  size_t smem = (size_t)w * w * sizeof(float) + (size_t)PK_RB * w * sizeof(float);
+  const size_t sub = (size_t)16 * 16 * params->sub_pix_reg * sizeof(float2);
+  if (params->sub_pix_reg > 1 && (size_t)w * w * sizeof(float) < sub) smem = sub + (size_t)PK_RB * w * sizeof(float);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_peaks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_peaks attr"));
+  k_peaks<<<M, PK_T, smem, (cudaStream_t)stream>>>(cwin, max_shift, *params, results, tw);
+  return launched("k_peaks");
+}

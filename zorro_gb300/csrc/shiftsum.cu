@@ -1,0 +1,92 @@
+// Shift every frame and sum (applyShifts, zorro.py:1734-1808, with
+// lanczosIndexedShift, zorro_util.py:341-379), plus the even/odd half sums of
+// lazyFouRingCorr (zorro.py:2237-2238), in one pass over the raw frames.
+//
+// Frame n is rolled by (roll_y, roll_x) (np.roll: out[i] = in[i - shift],
+// circular), then convolved with the separable 3x3 kernel ky (x) kx
+// (scipy.ndimage.convolve: out[i] = sum_k w[k] in[i - k + 1], 'reflect'
+// borders of the rolled frame).  Sums run over frames in order in float32,
+// as np.sum(images, axis=0) does for a float32 stack.
+#include "common.cuh"
+#include "internal.h"
+
+namespace zr {
+
+constexpr int SS_TX = 64, SS_TY = 16, SS_THR = 256;
+
+__device__ __forceinline__ int refl1(int i, int n) { return i < 0 ? -i - 1 : (i >= n ? 2 * n - i - 1 : i); }
+
+__global__ void __launch_bounds__(SS_THR)
+    k_shift_sum(FrameSrc f, const zr_shift_t* __restrict__ sh, float* __restrict__ sum,
+                float* __restrict__ even, float* __restrict__ odd, float* __restrict__ aligned) {
+  __shared__ float tile[SS_TY + 2][SS_TX + 2];
+  const int x0 = blockIdx.x * SS_TX, y0 = blockIdx.y * SS_TY;
+  const int tx = threadIdx.x & (SS_TX - 1), ty = threadIdx.x / SS_TX;  // ty in [0,4)
+  constexpr int RPT = SS_TY / (SS_THR / SS_TX);                            // rows per thread (4)
+  float s[RPT], se[RPT], so[RPT];
+#pragma unroll
+  for (int i = 0; i < RPT; i++) s[i] = se[i] = so[i] = 0.0f;
+  const int H = f.H, W = f.W;
+  for (int n = 0; n < f.N; n++) {
+    const zr_shift_t t = sh[n];
+    __syncthreads();
+    for (int e = threadIdx.x; e < (SS_TY + 2) * (SS_TX + 2); e += SS_THR) {
+      const int i = e / (SS_TX + 2), j = e - i * (SS_TX + 2);
+      const int Y = refl1(y0 - 1 + i, H), X = refl1(x0 - 1 + j, W);
+      float v = 0.0f;
+      if (y0 - 1 + i < H + 1 && x0 - 1 + j < W + 1) {
+        int sy = (Y - t.roll_y) % H;
+        if (sy < 0) sy += H;
+        int sx = (X - t.roll_x) % W;
+        if (sx < 0) sx += W;
+        v = load_corrected(f, n, sy, sx);
+      }
+      tile[i][j] = v;
+    }
+    __syncthreads();
+    const int x = x0 + tx;
+#pragma unroll
+    for (int i = 0; i < RPT; i++) {
+      const int y = y0 + ty * RPT + i;
+      float a;
+      const int ly = ty * RPT + i + 1, lx = tx + 1;
+      if (t.apply) {
+        // sum_a ky[a] sum_b kx[b] R(y - a + 1, x - b + 1)
+        float r0 = fmaf(t.kx[0], tile[ly + 1][lx + 1], fmaf(t.kx[1], tile[ly + 1][lx], t.kx[2] * tile[ly + 1][lx - 1]));
+        float r1 = fmaf(t.kx[0], tile[ly][lx + 1], fmaf(t.kx[1], tile[ly][lx], t.kx[2] * tile[ly][lx - 1]));
+        float r2 = fmaf(t.kx[0], tile[ly - 1][lx + 1], fmaf(t.kx[1], tile[ly - 1][lx], t.kx[2] * tile[ly - 1][lx - 1]));
+        a = fmaf(t.ky[0], r0, fmaf(t.ky[1], r1, t.ky[2] * r2));
+      } else {
+        a = tile[ly][lx];
+      }
+      s[i] += a;
+      if (n & 1) so[i] += a; else se[i] += a;
+      if (aligned && y < H && x < W) aligned[(size_t)n * H * W + (size_t)y * W + x] = a;
+    }
+  }
+  const int x = x0 + tx;
+#pragma unroll
+  for (int i = 0; i < RPT; i++) {
+    const int y = y0 + ty * RPT + i;
+    if (y < H && x < W) {
+      const size_t p = (size_t)y * W + x;
+      sum[p] = s[i];
+      if (even) even[p] = se[i];
+      if (odd) odd[p] = so[i];
+    }
+  }
+}
+
+}  // namespace zr
+
+using namespace zr;
+
+extern "C" int zr_shift_sum(const zr_frames_t* frames, const zr_shift_t* shifts, float* image_sum, float* even_sum,
+                            float* odd_sum, float* aligned, void* stream) {
+  if (!frames || !frames->raw || !shifts || !image_sum) return set_error(ZR_EINVAL, "zr_shift_sum: null argument");
+  FrameSrc f = make_src(frames);
+  if (f.N <= 0 || f.H < 2 || f.W < 2) return set_error(ZR_EINVAL, "zr_shift_sum: empty movie");
+  dim3 grid((f.W + SS_TX - 1) / SS_TX, (f.H + SS_TY - 1) / SS_TY);
+  k_shift_sum<<<grid, SS_THR, 0, (cudaStream_t)stream>>>(f, shifts, image_sum, even_sum, odd_sum, aligned);
+  return launched("k_shift_sum");
+}

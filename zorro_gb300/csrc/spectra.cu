@@ -1,0 +1,216 @@
+// Forward spectra of the masked frames (xcorrnm2_tri, zorro.py:814-925).
+//
+// The reference transforms m*I and (m*I)^2 as two complex P0 x P1 FFTs per
+// frame and keeps the four corners (FFTCrop, zorro.py:901-914).  Here both
+// real images go through ONE complex FFT per row (z = u + i u^2, untangled by
+// Hermitian symmetry), only the C1/2+1 non-negative kx columns the crop keeps
+// are written, and the column pass keeps only the C0+1 cropped ky rows.
+//
+// Row-pass output layout (scratch): [frame][y/4][K4][y%4] complex, so that
+// the row pass (4 rows per CTA) and the column pass (4 columns per CTA) both
+// move whole 128-byte lines.
+#include <stdio.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace zr {
+
+constexpr int NBR = 4;  // rows / columns per CTA
+
+template <int P1>
+__global__ void __launch_bounds__(fft_threads(P1, NBR))
+    k_fwd_rows(FrameSrc f, const float* __restrict__ mask, const double* __restrict__ mean_sub,
+               double inv_area, int frame0, int mode, int rows, int cols, int C1, int K4, int H4,
+               float2* __restrict__ RU, float2* __restrict__ RV, const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(P1, NBR);
+  constexpr int LD = ld_of(P1);
+  extern __shared__ float2 sm[];
+  const int g = blockIdx.x;
+  const int nl = blockIdx.y;
+  const int n = frame0 + nl;
+  float mu = 0.0f;
+  if (mode == 0 && mean_sub) mu = (float)(mean_sub[n] * inv_area);
+  for (int e = threadIdx.x; e < NBR * P1; e += T) {
+    const int r = e / P1, x = e - (e / P1) * P1;
+    const int y = g * NBR + r;
+    float2 z = make_float2(0.0f, 0.0f);
+    if (y < rows && x < cols) {
+      const float m = mask ? __ldg(mask + (size_t)y * P1 + x) : 1.0f;
+      if (mode == 0) {
+        const float u = m * (load_corrected(f, n, y, x) - mu);
+        z = make_float2(u, u * u);
+      } else {
+        z.x = m;
+      }
+    }
+    sm[r * LD + pidx(x)] = z;
+  }
+  __syncthreads();
+  block_fft<P1, NBR, T, -1>(sm, tw);
+  const size_t base = ((size_t)nl * H4 + g) * K4 * NBR;
+  const int half = C1 / 2;
+  for (int e = threadIdx.x; e < K4 * NBR; e += T) {
+    const int k = e / NBR, r = e - (e / NBR) * NBR;
+    float2 U = make_float2(0.0f, 0.0f), V = U;
+    if (k <= half) {
+      const float2 zk = sm[r * LD + pidx(k)];
+      const float2 zm = sm[r * LD + pidx((P1 - k) & (P1 - 1))];
+      U = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      V = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    }
+    RU[base + e] = U;
+    if (mode == 0) RV[base + e] = V;
+  }
+}
+
+template <int P0>
+__global__ void __launch_bounds__(fft_threads(P0, NBR))
+    k_fwd_cols(const float2* __restrict__ RU, const float2* __restrict__ RV, int rows, int C0, int K4, int H4,
+               long long spec_elems, float2* __restrict__ G, float2* __restrict__ S,
+               const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(P0, NBR);
+  constexpr int LD = ld_of(P0);
+  extern __shared__ float2 sm[];
+  const int k0 = blockIdx.x * NBR;
+  const int nl = blockIdx.y;
+  const float2* R = (blockIdx.z == 0 ? RU : RV) + (size_t)nl * H4 * K4 * NBR;
+  float2* out = (blockIdx.z == 0 ? G : S) + (size_t)nl * spec_elems;
+  for (int e = threadIdx.x; e < H4 * NBR * NBR; e += T) {
+    const int gg = e / (NBR * NBR), j = e - gg * (NBR * NBR);
+    const int c = j / NBR, r = j - c * NBR;
+    const int y = gg * NBR + r;
+    float2 v = R[((size_t)gg * K4 + k0) * NBR + j];
+    if (y >= rows) v = make_float2(0.0f, 0.0f);
+    sm[c * LD + pidx(y)] = v;
+  }
+  for (int e = threadIdx.x; e < (P0 - H4 * NBR) * NBR; e += T) {
+    const int c = e / (P0 - H4 * NBR), y = H4 * NBR + e - c * (P0 - H4 * NBR);
+    sm[c * LD + pidx(y)] = make_float2(0.0f, 0.0f);
+  }
+  __syncthreads();
+  block_fft<P0, NBR, T, -1>(sm, tw);
+  const int hc = C0 / 2;
+  for (int e = threadIdx.x; e < (C0 + 1) * NBR; e += T) {
+    const int r = e / NBR, c = e - r * NBR;
+    const int ky = r < hc ? r : (r < C0 ? P0 - C0 + r : hc);
+    out[(size_t)r * K4 + k0 + c] = sm[c * LD + pidx(ky)];
+  }
+}
+
+__global__ void k_frame_sums(FrameSrc f, double* __restrict__ sums) {
+  const int n = blockIdx.y;
+  const long long npix = (long long)f.H * f.W;
+  float acc = 0.0f;
+  double dacc = 0.0;
+  int cnt = 0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(p / f.W), x = (int)(p - (long long)y * f.W);
+    acc += load_corrected(f, n, y, x);
+    if (++cnt == 64) { dacc += acc; acc = 0.0f; cnt = 0; }
+  }
+  dacc += acc;
+  for (int o = 16; o > 0; o >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dacc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) atomicAdd(sums + n, v);
+  }
+}
+
+template <int P>
+static int launch_rows(const FrameSrc& f, const float* mask, const double* mean_sub, double inv_area,
+                       int frame0, int nfr, int mode, int rows, int cols, int C1, int K4, int H4,
+                       float2* RU, float2* RV, const float2* tw, cudaStream_t st) {
+  constexpr int T = fft_threads(P, NBR);
+  const size_t smem = (size_t)NBR * ld_of(P) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_rows<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_fwd_rows attr"));
+  k_fwd_rows<P><<<dim3(H4, nfr), T, smem, st>>>(f, mask, mean_sub, inv_area, frame0, mode, rows, cols, C1, K4,
+                                                 H4, RU, RV, tw);
+  return launched("k_fwd_rows");
+}
+
+template <int P>
+static int launch_cols(const float2* RU, const float2* RV, int rows, int C0, int K4, int H4, long long se,
+                       int nfr, int nz, float2* G, float2* S, const float2* tw, cudaStream_t st) {
+  constexpr int T = fft_threads(P, NBR);
+  const size_t smem = (size_t)NBR * ld_of(P) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_cols<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_fwd_cols attr"));
+  k_fwd_cols<P><<<dim3(K4 / NBR, nfr, nz), T, smem, st>>>(RU, RV, rows, C0, K4, H4, se, G, S, tw);
+  return launched("k_fwd_cols");
+}
+
+#define ZR_POW2_DISPATCH(L, CALL)                  \
+  switch (L) {                                     \
+    case 64: { constexpr int LL = 64; CALL; } break;     \
+    case 128: { constexpr int LL = 128; CALL; } break;   \
+    case 256: { constexpr int LL = 256; CALL; } break;   \
+    case 512: { constexpr int LL = 512; CALL; } break;   \
+    case 1024: { constexpr int LL = 1024; CALL; } break; \
+    case 2048: { constexpr int LL = 2048; CALL; } break; \
+    case 4096: { constexpr int LL = 4096; CALL; } break; \
+    default: return set_error(ZR_ESIZE, "transform length %d not supported (powers of two 64..4096)", (int)(L)); \
+  }
+
+}  // namespace zr
+
+using namespace zr;
+
+extern "C" int zr_spectrum_pitch(int C1) { return ((C1 / 2 + 1) + 3) & ~3; }
+
+extern "C" long long zr_spectrum_elems(int C0, int C1) { return (long long)(C0 + 1) * zr_spectrum_pitch(C1); }
+
+extern "C" size_t zr_spectra_work_bytes(int height, int n_frames, int C1) {
+  const size_t H4 = (size_t)(height + 3) / 4;
+  return 2 * (size_t)n_frames * H4 * zr_spectrum_pitch(C1) * 4 * sizeof(float2);
+}
+
+extern "C" int zr_frame_sums(const zr_frames_t* frames, double* sums, void* stream) {
+  if (!frames || !sums || !frames->raw) return set_error(ZR_EINVAL, "zr_frame_sums: null argument");
+  FrameSrc f = make_src(frames);
+  if (f.N <= 0 || f.H <= 0 || f.W <= 0) return set_error(ZR_EINVAL, "zr_frame_sums: empty movie");
+  const long long npix = (long long)f.H * f.W;
+  int bx = (int)((npix + 256 * 64 - 1) / (256 * 64));
+  if (bx > 1024) bx = 1024;
+  k_frame_sums<<<dim3(bx, f.N), 256, 0, (cudaStream_t)stream>>>(f, sums);
+  return launched("k_frame_sums");
+}
+
+extern "C" int zr_spectra(const zr_frames_t* frames, const float* mask, const double* mean_sub, int frame0,
+                          int n_frames, int mode, int P0, int P1, int C0, int C1, void* G, void* S, void* work,
+                          size_t work_bytes, void* stream) {
+  if (!frames || !G || (mode == 0 && (!S || !frames->raw)))
+    return set_error(ZR_EINVAL, "zr_spectra: null argument");
+  if (!is_pow2(P0) || !is_pow2(P1) || !is_pow2(C0) || !is_pow2(C1) || C0 > P0 || C1 > P1 || C0 < 64 || C1 < 64)
+    return set_error(ZR_ESIZE, "zr_spectra: P=%dx%d C=%dx%d must be powers of two with 64 <= C <= P <= 4096", P0,
+                     P1, C0, C1);
+  FrameSrc f = make_src(frames);
+  if (f.H > P0 || f.W > P1) return set_error(ZR_EINVAL, "zr_spectra: frame %dx%d larger than padded %dx%d", f.H, f.W, P0, P1);
+  if (n_frames <= 0 || frame0 < 0 || (mode == 0 && frame0 + n_frames > f.N))
+    return set_error(ZR_EINVAL, "zr_spectra: frame range [%d,%d) outside movie of %d frames", frame0, frame0 + n_frames, f.N);
+  const int rows = (mode == 1 && mask) ? P0 : f.H;
+  const int cols = (mode == 1 && mask) ? P1 : f.W;
+  const int H4 = (rows + 3) / 4;
+  const int K4 = zr_spectrum_pitch(C1);
+  const size_t need = (size_t)(mode == 0 ? 2 : 1) * n_frames * H4 * K4 * 4 * sizeof(float2);
+  if (!work || work_bytes < need)
+    return set_error(ZR_EWORK, "zr_spectra: work buffer %zu bytes < %zu needed", work_bytes, need);
+  const float2* tw = twiddles();
+  if (!tw) return ZR_ECUDA;
+  float2* RU = (float2*)work;
+  float2* RV = RU + (size_t)n_frames * H4 * K4 * 4;
+  cudaStream_t st = (cudaStream_t)stream;
+  const double inv_area = 1.0 / ((double)f.H * f.W);
+  ZR_POW2_DISPATCH(P1, ZR_TRY((launch_rows<LL>(f, mask, mean_sub, inv_area, frame0, n_frames, mode, rows, cols, C1,
+                                                K4, H4, RU, RV, tw, st))));
+  const long long se = zr_spectrum_elems(C0, C1);
+  ZR_POW2_DISPATCH(P0, ZR_TRY((launch_cols<LL>(RU, RV, rows, C0, K4, H4, se, n_frames, mode == 0 ? 2 : 1,
+                                                (float2*)G, (float2*)S, tw, st))));
+  return ZR_OK;
+}

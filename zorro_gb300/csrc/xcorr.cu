@@ -1,0 +1,241 @@
+// Masked normalised cross-correlation windows (mnxc2, zorro.py:1014-1097).
+//
+// Every term of mnxc2 is real(IFFT_C(A * conj(B))) for two cropped spectra A
+// and B of real images, and only the +/-maxShift window of it is ever used
+// (zorro.py:1090-1092).  With the half-plane spectra of zr_spectra:
+//
+//   column pass  for each kx in [0, C1/2]: build the C0 products of column kx
+//                exactly as the full C0 x C1 cropped product would contribute
+//                to real(IFFT) (the Nyquist row/column of the crop is not its
+//                own Hermitian mirror, so row ky=-C0/2 averages the -C0/2 and
+//                +C0/2 products and column kx=C1/2 uses the mirrored -C1/2
+//                values), inverse FFT of length C0, keep the w window rows;
+//   row pass     two window rows packed into one complex inverse FFT of length
+//                C1 (real-output trick), keep the w window columns, scale by
+//                normConst2 / (C0*C1) (zorro.py:634 and numpy's 1/N).
+//
+// The four frame-only terms (CorrTM, CorrBM and the two Denominator IFFTs)
+// depend on one frame each, so they are computed once per frame (zr_xcorr_terms)
+// instead of once per pair; the pair kernel only transforms the numerator
+// G_J conj(G_I) and combines.
+#include "common.cuh"
+#include "internal.h"
+
+namespace zr {
+
+constexpr int XC_NBC = 4;  // columns per CTA in the column pass
+constexpr int XC_NBR = 2;  // packed row pairs per CTA in the row pass
+
+struct XcJobs {
+  const float2* G;
+  const float2* S;
+  const float2* GM;
+  const int* pairs;  // kind 1
+  int N;
+  int kind;          // 0 terms, 1 pairs
+  int job0;
+  long long se;      // spectrum elements
+};
+
+__device__ __forceinline__ void job_operands(const XcJobs& J, int job, const float2*& A, const float2*& B) {
+  if (J.kind == 1) {
+    const int I = J.pairs[2 * job], Jj = J.pairs[2 * job + 1];
+    A = J.G + (size_t)Jj * J.se;
+    B = J.G + (size_t)I * J.se;
+    return;
+  }
+  const int t = job / J.N, n = job - t * J.N;
+  switch (t) {
+    case 0: A = J.GM; B = J.G + (size_t)n * J.se; break;   // CorrTM: M * conj(G_I)
+    case 1: A = J.G + (size_t)n * J.se; B = J.GM; break;   // CorrBM: conj(M) * G_J
+    case 2: A = J.GM; B = J.S + (size_t)n * J.se; break;   // DenomT: M * conj(S_I)
+    case 3: A = J.S + (size_t)n * J.se; B = J.GM; break;   // DenomB: conj(M) * S_J
+    default: A = J.GM; B = J.GM; break;                     // maskProduct
+  }
+}
+
+template <int C0>
+__global__ void __launch_bounds__(fft_threads(C0, XC_NBC))
+    k_xc_cols(XcJobs J, int C1, int K4, int mS, float2* __restrict__ Tw, const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(C0, XC_NBC);
+  constexpr int LD = ld_of(C0);
+  extern __shared__ float2 sm[];
+  const int k0 = blockIdx.x * XC_NBC;
+  const int jl = blockIdx.y;
+  const float2 *A, *B;
+  job_operands(J, J.job0 + jl, A, B);
+  const int half = C1 / 2, hc = C0 / 2;
+  for (int e = threadIdx.x; e < C0 * XC_NBC; e += T) {
+    const int r = e / XC_NBC, c = e - r * XC_NBC;
+    const int k = k0 + c;
+    float2 h = make_float2(0.0f, 0.0f);
+    if (k == 0) {
+      h = cmulc(A[(size_t)r * K4], B[(size_t)r * K4]);
+    } else if (k < half) {
+      h = cmulc(A[(size_t)r * K4 + k], B[(size_t)r * K4 + k]);
+      if (r == hc) {
+        const float2 h2 = cmulc(A[(size_t)C0 * K4 + k], B[(size_t)C0 * K4 + k]);
+        h = make_float2(0.5f * (h.x + h2.x), 0.5f * (h.y + h2.y));
+      }
+    } else if (k == half) {
+      const int m = (r == 0) ? 0 : (r == hc ? C0 : C0 - r);
+      h = cmulc(B[(size_t)m * K4 + k], A[(size_t)m * K4 + k]);  // conj(A) * B
+    }
+    sm[c * LD + pidx(r)] = h;
+  }
+  __syncthreads();
+  block_fft<C0, XC_NBC, T, 1>(sm, tw);
+  const int w = 2 * mS;
+  float2* out = Tw + (size_t)jl * w * K4;
+  for (int e = threadIdx.x; e < w * XC_NBC; e += T) {
+    const int a = e / XC_NBC, c = e - a * XC_NBC;
+    const int y = (a - mS) & (C0 - 1);
+    out[(size_t)a * K4 + k0 + c] = sm[c * LD + pidx(y)];
+  }
+}
+
+template <int C1>
+__global__ void __launch_bounds__(fft_threads(C1, XC_NBR))
+    k_xc_rows(XcJobs J, int C0, int K4, int mS, float scale, const float2* __restrict__ Tw,
+              const float* __restrict__ terms, float* __restrict__ out, const float2* __restrict__ tw) {
+  constexpr int T = fft_threads(C1, XC_NBR);
+  constexpr int LD = ld_of(C1);
+  constexpr int half = C1 / 2;
+  extern __shared__ float2 sm[];
+  const int w = 2 * mS;
+  const int jl = blockIdx.y;
+  const int job = J.job0 + jl;
+  const int arow0 = blockIdx.x * (2 * XC_NBR);
+  const float2* src = Tw + (size_t)jl * w * K4;
+  for (int e = threadIdx.x; e < XC_NBR * (half + 1); e += T) {
+    const int p = e / (half + 1), k = e - p * (half + 1);
+    const int a0 = arow0 + 2 * p, a1 = a0 + 1;
+    const float2 ga = a0 < w ? src[(size_t)a0 * K4 + k] : make_float2(0.0f, 0.0f);
+    const float2 gb = a1 < w ? src[(size_t)a1 * K4 + k] : make_float2(0.0f, 0.0f);
+    float2* s = sm + p * LD;
+    if (k == 0 || k == half) {
+      s[pidx(k)] = make_float2(ga.x, gb.x);
+    } else {
+      s[pidx(k)] = make_float2(ga.x - gb.y, ga.y + gb.x);           // ga + i gb
+      s[pidx(C1 - k)] = make_float2(ga.x + gb.y, -ga.y + gb.x);     // conj(ga) + i conj(gb)
+    }
+  }
+  __syncthreads();
+  block_fft<C1, XC_NBR, T, 1>(sm, tw);
+  const size_t w2 = (size_t)w * w;
+  for (int e = threadIdx.x; e < XC_NBR * 2 * w; e += T) {
+    const int q = e / w, b = e - q * w;
+    const int p = q >> 1;
+    const int a = arow0 + q;
+    if (a >= w) continue;
+    const int x = (b - mS) & (C1 - 1);
+    const float2 yv = sm[p * LD + pidx(x)];
+    const float v = ((q & 1) ? yv.y : yv.x) * scale;
+    const size_t pix = (size_t)a * w + b;
+    if (J.kind == 0) {
+      out[(size_t)job * w2 + pix] = v;
+    } else {
+      const int I = J.pairs[2 * job], Jj = J.pairs[2 * job + 1];
+      const int N = J.N;
+      const float ctm = terms[(size_t)I * w2 + pix];
+      const float cbm = terms[(size_t)(N + Jj) * w2 + pix];
+      const float dt = terms[(size_t)(2 * N + I) * w2 + pix];
+      const float db = terms[(size_t)(3 * N + Jj) * w2 + pix];
+      const float mp = terms[(size_t)(4 * N) * w2 + pix];
+      float den = sqrtf((db - cbm * (cbm / mp)) * (dt - ctm * (ctm / mp)));
+      den = (den < 1.0f) ? 1.0f : den;  // np.clip(Denom, 1, inf); NaN stays NaN
+      out[(size_t)job * w2 + pix] = (v - ctm * cbm / mp) / den;
+    }
+  }
+}
+
+template <int C0>
+static int launch_xc_cols(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
+                          cudaStream_t st) {
+  constexpr int T = fft_threads(C0, XC_NBC);
+  const size_t smem = (size_t)XC_NBC * ld_of(C0) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_xc_cols attr"));
+  k_xc_cols<C0><<<dim3(K4 / XC_NBC, nj), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
+  return launched("k_xc_cols");
+}
+
+template <int C1>
+static int launch_xc_rows(const XcJobs& J, int nj, int C0, int K4, int mS, float scale, const float2* Tw,
+                          const float* terms, float* out, const float2* tw, cudaStream_t st) {
+  constexpr int T = fft_threads(C1, XC_NBR);
+  const size_t smem = (size_t)XC_NBR * ld_of(C1) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_rows<C1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_xc_rows attr"));
+  const int w = 2 * mS;
+  k_xc_rows<C1><<<dim3((w + 2 * XC_NBR - 1) / (2 * XC_NBR), nj), T, smem, st>>>(J, C0, K4, mS, scale, Tw, terms,
+                                                                               out, tw);
+  return launched("k_xc_rows");
+}
+
+#define ZR_XC_DISPATCH(L, CALL)                               \
+  switch (L) {                                                \
+    case 64: { constexpr int LL = 64; CALL; } break;          \
+    case 128: { constexpr int LL = 128; CALL; } break;        \
+    case 256: { constexpr int LL = 256; CALL; } break;        \
+    case 512: { constexpr int LL = 512; CALL; } break;        \
+    case 1024: { constexpr int LL = 1024; CALL; } break;      \
+    case 2048: { constexpr int LL = 2048; CALL; } break;      \
+    case 4096: { constexpr int LL = 4096; CALL; } break;      \
+    default: return set_error(ZR_ESIZE, "crop size %d not supported", (int)(L)); \
+  }
+
+static int run_jobs(XcJobs J, int njobs, int C0, int C1, int mS, const float* terms, float* out, void* work,
+                    size_t work_bytes, cudaStream_t st) {
+  const int K4 = zr_spectrum_pitch(C1);
+  const int w = 2 * mS;
+  const size_t per_job = (size_t)w * K4 * sizeof(float2);
+  if (!work || work_bytes < per_job)
+    return set_error(ZR_EWORK, "zr_xcorr: work buffer %zu bytes < %zu (one job)", work_bytes, per_job);
+  const int wave = (int)((work_bytes / per_job) < (size_t)njobs ? work_bytes / per_job : (size_t)njobs);
+  const float2* tw = twiddles();
+  if (!tw) return ZR_ECUDA;
+  const double nc2 = (double)(float)(1.0 / (((double)C0 * C1) * ((double)C0 * C1)));
+  const float scale = (float)(nc2 / ((double)C0 * C1));
+  float2* Tw = (float2*)work;
+  for (int j0 = 0; j0 < njobs; j0 += wave) {
+    const int nj = (njobs - j0) < wave ? (njobs - j0) : wave;
+    J.job0 = j0;
+    ZR_XC_DISPATCH(C0, ZR_TRY((launch_xc_cols<LL>(J, nj, C1, K4, mS, Tw, tw, st))));
+    ZR_XC_DISPATCH(C1, ZR_TRY((launch_xc_rows<LL>(J, nj, C0, K4, mS, scale, Tw, terms, out, tw, st))));
+  }
+  return ZR_OK;
+}
+
+static int check_sizes(int C0, int C1, int mS) {
+  if (!is_pow2(C0) || !is_pow2(C1) || C0 < 64 || C1 < 64 || C0 > 4096 || C1 > 4096)
+    return set_error(ZR_ESIZE, "crop %dx%d must be powers of two in [64, 4096]", C0, C1);
+  if (mS < 2 || 2 * mS > C0 || 2 * mS > C1 || mS > 112)
+    return set_error(ZR_ESIZE, "maxShift %d must satisfy 2 <= maxShift <= min(112, C/2)", mS);
+  return ZR_OK;
+}
+
+}  // namespace zr
+
+using namespace zr;
+
+extern "C" size_t zr_xcorr_work_bytes(int n_jobs, int C1, int max_shift) {
+  return (size_t)n_jobs * 2 * max_shift * zr_spectrum_pitch(C1) * sizeof(float2);
+}
+
+extern "C" int zr_xcorr_terms(const void* G, const void* S, const void* GM, int N, int C0, int C1, int max_shift,
+                              float* terms, void* work, size_t work_bytes, void* stream) {
+  if (!G || !S || !GM || !terms || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_terms: null argument");
+  ZR_TRY(check_sizes(C0, C1, max_shift));
+  XcJobs J{(const float2*)G, (const float2*)S, (const float2*)GM, nullptr, N, 0, 0, zr_spectrum_elems(C0, C1)};
+  return run_jobs(J, 4 * N + 1, C0, C1, max_shift, nullptr, terms, work, work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int zr_xcorr_pairs(const void* G, const float* terms, const int* pairs, int M, int N, int C0, int C1,
+                              int max_shift, float* cwin, void* work, size_t work_bytes, void* stream) {
+  if (!G || !terms || !pairs || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_pairs: null argument");
+  if (M <= 0) return ZR_OK;
+  ZR_TRY(check_sizes(C0, C1, max_shift));
+  XcJobs J{(const float2*)G, nullptr, nullptr, pairs, N, 1, 0, zr_spectrum_elems(C0, C1)};
+  return run_jobs(J, M, C0, C1, max_shift, terms, cwin, work, work_bytes, (cudaStream_t)stream);
+}

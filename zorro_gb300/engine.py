@@ -1,0 +1,437 @@
+"""The GPU pipeline behind ``ImageRegistrator.alignImageStack``.
+
+One ``Engine`` per device owns the stream and a pool of device buffers
+(PyTorch tensors, grown on demand and reused across movies); every pass over
+pixels is a ``libzorrogb`` entry point.  Host work is limited to the float64
+fits of ``hostmath`` and happens at three points where the reference's own
+logic needs scalars: the hot-pixel histogram fit, the drift solve, and the
+per-frame dose constants.
+
+Two exact reformulations of the reference's arithmetic are used:
+
+* each frame's mean (over the image area) is subtracted before the forward
+  transforms when the mask is the default padStack mask.  The masked
+  normalised correlation of zorro.py:1034-1074 is invariant to adding a
+  constant inside a binary mask (the numerator minus CorrTM*CorrBM/maskProduct
+  and both Denominator terms are covariances), so this changes only rounding:
+  it removes the large mean-times-mean term that float32 would otherwise
+  cancel;
+* the four frame-only IFFTs of mnxc2 are computed once per frame, not once
+  per pair.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib
+from . import hostmath as hm
+from ._lib import Frames, HotpixParams, PeakParams, PeakResult, Shift, DoseParams
+
+_RAW_TYPES = {np.dtype(np.float32): _lib.ZR_F32, np.dtype(np.uint8): _lib.ZR_U8, np.dtype(np.uint16): _lib.ZR_U16,
+              np.dtype(np.float16): _lib.ZR_F16}
+
+# scratch budgets (bytes) for the staged passes
+SPECTRA_WORK = 512 << 20
+XCORR_WORK = 256 << 20
+DOSE_WORK = 1536 << 20
+
+
+def _pow2(v):
+    return v > 0 and (v & (v - 1)) == 0
+
+
+class Engine:
+    _engines = {}
+
+    @classmethod
+    def get(cls, device=0):
+        e = cls._engines.get(device)
+        if e is None:
+            e = cls._engines[device] = Engine(device)
+        return e
+
+    def __init__(self, device=0):
+        import torch
+        if not torch.cuda.is_available():
+            raise _lib.ZorroError("no CUDA device: the GB300 registration path has no CPU fallback")
+        self.torch = torch
+        self.device = device
+        self.dev = torch.device("cuda", device)
+        self.lib = _lib.load()
+        with torch.cuda.device(self.dev):
+            _lib.call("zr_init", device)
+        self.bufs = {}
+        self.profile = None  # dict stage -> list of (start, end) CUDA events when enabled
+
+    def call(self, stage, name, *args):
+        """One C-ABI call; bracketed by CUDA events on the current stream when
+        profiling is on (self.profile is a dict)."""
+        if self.profile is None:
+            return _lib.call(name, *args)
+        torch = self.torch
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = _lib.call(name, *args)
+        e1.record()
+        self.profile.setdefault(stage, []).append((e0, e1))
+        return rc
+
+    def stage_ms(self):
+        """Summed device time per stage of the recorded calls (synchronises)."""
+        self.torch.cuda.synchronize(self.dev)
+        return {k: sum(a.elapsed_time(b) for a, b in v) for k, v in (self.profile or {}).items()}
+
+    # ------------------------------------------------------------------ buffers
+    def buf(self, name, nbytes):
+        t = self.bufs.get(name)
+        if t is None or t.numel() < nbytes:
+            t = self.torch.empty(max(int(nbytes), 1), dtype=self.torch.uint8, device=self.dev)
+            self.bufs[name] = t
+        return t
+
+    def ptr(self, name, nbytes):
+        return self.buf(name, nbytes).data_ptr()
+
+    def tensor(self, name, shape, dtype):
+        torch = self.torch
+        n = int(np.prod(shape)) * torch.empty(0, dtype=dtype).element_size()
+        return self.buf(name, n)[:n].view(dtype).view(*shape)
+
+    @property
+    def stream(self):
+        return self.torch.cuda.current_stream(self.dev).cuda_stream
+
+    # ------------------------------------------------------------------ input
+    def upload(self, reg):
+        torch = self.torch
+        imgs = reg.images
+        if isinstance(imgs, torch.Tensor):
+            t = imgs.to(self.dev, non_blocking=True)
+            dt = np.dtype(str(t.dtype).replace("torch.", ""))
+        else:
+            a = np.ascontiguousarray(imgs)
+            if a.dtype == np.float64:
+                a = a.astype(np.float32)
+            dt = a.dtype
+            t = torch.from_numpy(a).to(self.dev, non_blocking=True)
+        if t.ndim != 3:
+            raise ValueError("zorro.alignImageStack: stacks must be 3D data")
+        if dt not in _RAW_TYPES:
+            raise ValueError("images dtype %s not supported (float32, uint8, uint16, float16)" % dt)
+        t = t.contiguous()
+        gain = None
+        if reg.gainRef is not None and dt != np.dtype(np.float32):
+            g = reg.gainRef
+            gain = (g.to(self.dev) if isinstance(g, torch.Tensor) else torch.from_numpy(
+                np.ascontiguousarray(g, dtype=np.float32)).to(self.dev, non_blocking=True)).float().contiguous()
+            if tuple(gain.shape) != tuple(t.shape[1:]):
+                raise ValueError("gainRef shape %s does not match frames %s" % (tuple(gain.shape), tuple(t.shape[1:])))
+        return t, gain, _RAW_TYPES[dt]
+
+    # ------------------------------------------------------------------ pipeline
+    def align(self, reg):
+        torch = self.torch
+        with torch.cuda.device(self.dev):
+            res = self._align(reg)
+        for k, v in res.items():
+            setattr(reg, k, v)
+
+    def _frames(self, raw, rtype, gain, ha=None, hb=None, gdiv=0.0):
+        N, H, W = raw.shape
+        return Frames(raw.data_ptr(), rtype, gain.data_ptr() if gain is not None else None,
+                      ha.data_ptr() if ha is not None else None, hb.data_ptr() if hb is not None else None,
+                      float(gdiv), N, H, W, 0)
+
+    def _align(self, reg):
+        torch = self.torch
+        st = self.stream
+        bench = {}
+        bench["align0"] = time.time()
+        if reg.preShift:
+            raise ValueError("preShift is not supported by the GPU path")
+        if reg.triMode == "refine":
+            raise ValueError("triMode 'refine' is not supported by the GPU path")
+        if reg.shapeBinned is not None and np.any(reg.shapeBinned):
+            raise ValueError("shapeBinned (Fourier binning) is not supported by the GPU path yet")
+        raw, gain, rtype = self.upload(reg)
+        N, H, W = (int(s) for s in raw.shape)
+        gdiv = float(reg.gain) if (reg.gain and not np.isclose(reg.gain, 1.0) and rtype != _lib.ZR_F32) else 0.0
+        frames = self._frames(raw, rtype, gain, gdiv=gdiv)
+        hotinfo = dict(reg.hotpixInfo)
+        filt = [f for f in (reg.filterMode or "").lower().replace(" ", "").split(",") if f]
+
+        # ---- hot pixels (zorro.py:2497-2672)
+        ha = hb = None
+        if "hot" in filt:
+            bench["hot0"] = time.time()
+            usum = self.tensor("usum", (H, W), torch.float32)
+            tot = self.tensor("tot", (4,), torch.float64)
+            tot.zero_()
+            self.call("A_gain_sum", "zr_gain_sum", C.byref(frames), usum.data_ptr(), tot.data_ptr(), st)
+            sumMean, pstd, edges = hm.hotpix_bins(float(tot[0].item()) / (H * W), hotinfo["maxSigma"])
+            nb = len(edges) - 1
+            hist = self.tensor("hist", (nb + 4,), torch.int32)
+            hist.zero_()
+            self.call("A_gain_sum", "zr_histogram", usum.data_ptr(), H * W, float(edges[0]), nb, hist.data_ptr(), st)
+            h = hist[:nb].cpu().numpy().astype(np.int64)
+            mu, sg, cl, cu, info = hm.hotpix_fit(h, edges, sumMean, pstd, hotinfo)
+            hotinfo.update(info)
+            prm = HotpixParams()
+            prm.mu, prm.sigma = float(mu), float(sg)
+            prm.cutoff_lower, prm.cutoff_upper = float(cl), float(cu)
+            prm.logistic_k, prm.relax = float(np.float32(hotinfo["logisticK"])), float(np.float32(hotinfo["relax"]))
+            psf = hm.psf_kernel(hotinfo.get("psf", "K2")).ravel()
+            for i in range(9):
+                prm.psf[i] = float(psf[i])
+            prm.neighbour_thres = 0.01
+            prm.best_mean = float(mu / N)
+            ha = self.tensor("hot_a", (H, W), torch.float32)
+            hb = self.tensor("hot_b", (H, W), torch.float32)
+            cnt = self.tensor("hotcnt", (4,), torch.int32)
+            cnt.zero_()
+            wb = self.lib.zr_hotpix_work_bytes(H, W)
+            self.call("B_hot_maps", "zr_hotpix_maps", usum.data_ptr(), H, W, N, C.byref(prm), ha.data_ptr(), hb.data_ptr(),
+                      cnt.data_ptr(), self.ptr("hotwork", wb), wb, st)
+            c = cnt.cpu().numpy()
+            hotinfo["guessDeadpix"] = int(c[0])
+            hotinfo["guessHotpix"] = int(c[1])
+            hotinfo["neighborPix"] = int(c[2])
+            hotinfo["frameMean"] = float(mu / N)
+            hotinfo["frameStd"] = float(sg / np.sqrt(N))
+            frames = self._frames(raw, rtype, gain, ha, hb, gdiv)
+            bench["hot1"] = time.time()
+
+        # ---- padding and crop sizes (padStack zorro.py:1908, __init_xcorrnm2 zorro.py:598-611)
+        if reg.shapePadded is not None and np.any(reg.shapePadded):
+            P0, P1 = int(reg.shapePadded[0]), int(reg.shapePadded[1])
+        else:
+            P0, P1 = H, W
+        if H > P0 or W > P1:
+            raise ValueError("shapePadded %s is smaller than the frames %s" % ([P0, P1], [H, W]))
+        if reg.fouCrop is not None and np.any(reg.fouCrop):
+            C0, C1 = (int(v) for v in 2 * np.floor(np.array(reg.fouCrop) / 2.0).astype(int))
+        else:
+            C0, C1 = P0, P1
+        for v, nm in ((P0, "shapePadded"), (P1, "shapePadded"), (C0, "fouCrop"), (C1, "fouCrop")):
+            if not _pow2(v):
+                raise ValueError("%s %d: the GPU path needs powers of two" % (nm, v))
+        mS = int(reg.maxShift)
+        w = 2 * mS
+        mask_dev = None
+        user_mask = reg.masks is not None and len(np.shape(reg.masks)) > 0
+        if user_mask:
+            m = np.asarray(reg.masks)
+            if m.ndim == 3 and m.shape[0] > 1:
+                raise ValueError("per-frame masks are not supported by the GPU path")
+            m = m.reshape(m.shape[-2], m.shape[-1]).astype(np.float32)
+            mp = np.zeros((P0, P1), np.float32)
+            mp[:m.shape[0], :m.shape[1]] = m
+            mask_dev = torch.from_numpy(mp).to(self.dev, non_blocking=True)
+        msub = None
+        if reg.subtractFrameMean and not user_mask:
+            msub = self.tensor("msub", (N,), torch.float64)
+            msub.zero_()
+            self.call("C_spectra", "zr_frame_sums", C.byref(frames), msub.data_ptr(), st)
+
+        # ---- spectra (xcorrnm2_tri zorro.py:814-925)
+        bench["xcorr0"] = time.time()
+        se = int(self.lib.zr_spectrum_elems(C0, C1))
+        G = self.tensor("G", (N, se, 2), torch.float32)
+        S = self.tensor("S", (N, se, 2), torch.float32)
+        GM = self.tensor("GM", (se, 2), torch.float32)
+        mrows = P0 if mask_dev is not None else H
+        wbm = self.lib.zr_spectra_work_bytes(mrows, 1, C1)
+        self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None, None, 0, 1,
+                  1, P0, P1, C0, C1, GM.data_ptr(), None, self.ptr("specwork", wbm), wbm, st)
+        per = self.lib.zr_spectra_work_bytes(H, 1, C1)
+        chunk = max(1, min(N, SPECTRA_WORK // per))
+        wb = per * chunk
+        wptr = self.ptr("specwork", wb)
+        for f0 in range(0, N, chunk):
+            nf = min(chunk, N - f0)
+            self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None,
+                      msub.data_ptr() if msub is not None else None, f0, nf, 0, P0, P1, C0, C1,
+                      G[f0].data_ptr(), S[f0].data_ptr(), wptr, wb, st)
+
+        # ---- correlation windows and peaks (mnxc2 / locatePeak)
+        tri = hm.tri_indices(N, reg.triMode, reg.diagWidth, reg.diagStart)
+        pairs = hm.pair_list(tri)
+        M = len(pairs)
+        terms = self.tensor("terms", (4 * N + 1, w, w), torch.float32)
+        xw = min(XCORR_WORK, max(self.lib.zr_xcorr_work_bytes(1, C1, mS), self.lib.zr_xcorr_work_bytes(M, C1, mS)))
+        xptr = self.ptr("xcwork", xw)
+        self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), N, C0, C1, mS, terms.data_ptr(), xptr,
+                  xw, st)
+        pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
+        cwin = self.tensor("cwin", (max(M, 1), w, w), torch.float32)
+        self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pairs_dev.data_ptr(), M, N, C0, C1, mS,
+                  cwin.data_ptr(), xptr, xw, st)
+        pp = PeakParams()
+        pp.sub_pix_reg = int(reg.subPixReg or 1)
+        bm = str(reg.Bmode)
+        if bm == "opti":
+            pp.bmode = 1
+        elif reg.Brad and bm in ("conv", "convolution"):
+            pp.bmode = 2
+            pp.conv_sigma_y = P0 / (np.sqrt(2) * np.pi * reg.Brad)
+            pp.conv_sigma_x = P1 / (np.sqrt(2) * np.pi * reg.Brad)
+        elif bm == "fourier":
+            raise ValueError("Bmode 'fourier' is broken in the reference (normConst undefined, zorro.py:1132)")
+        else:
+            pp.bmode = 0
+        pp.suppress_origin = int(bool(reg.suppressOrigin))
+        pp.use_mask = 1
+        pp.opti_lo, pp.opti_hi, pp.opti_xatol, pp.opti_maxiter = 0.0, 7.0, 0.01, 15
+        pres = self.tensor("peaks", (max(M, 1), C.sizeof(PeakResult)), torch.uint8)
+        self.call("F_peaks", "zr_locate_peaks", cwin.data_ptr(), M, mS, C.byref(pp), pres.data_ptr(), st)
+        host = pres[:M].cpu().numpy()
+        pr = np.frombuffer(host.tobytes(), dtype=np.dtype([("sy", "f8"), ("sx", "f8"), ("sigma", "f8"), ("corr", "f4"),
+                                                           ("peaksig", "f4"), ("origin", "f4"), ("cy", "i4"),
+                                                           ("cx", "i4"), ("flags", "i4"), ("nfev", "i4")],
+                                                          align=True))
+        bench["xcorr2"] = time.time()
+        shifts = np.zeros([N, N, 2])
+        corr = np.zeros([N, N])
+        psig = np.zeros([N, N])
+        orig = np.zeros([N, N])
+        keep = np.ones(M, dtype=bool)
+        if reg.triMode == "auto":
+            row_done = {}
+            for k, (I, J) in enumerate(pairs):
+                if row_done.get(I):
+                    keep[k] = False
+                    continue
+                if pr["peaksig"][k] <= reg.peaksigThres or J - I >= reg.autoMax:
+                    row_done[I] = True
+        Ii, Jj = pairs[keep, 0], pairs[keep, 1]
+        shifts[Ii, Jj, 0] = pr["sy"][keep]
+        shifts[Ii, Jj, 1] = pr["sx"][keep]
+        corr[Ii, Jj] = pr["corr"][keep]
+        psig[Ii, Jj] = pr["peaksig"][keep]
+        orig[Ii, Jj] = pr["origin"][keep]
+        if reg.fouCrop is not None and np.any(reg.fouCrop):
+            shifts[:, :, 0] *= P0 / C0
+            shifts[:, :, 1] *= P1 / C1
+        self.last_peaks = pr
+        self.last_pairs = pairs
+        bench["xcorr3"] = time.time()
+
+        # ---- drift solve (shiftsSolver zorro.py:1260-1567)
+        out = {}
+        edl = list(reg.errorDictList)
+        if reg.triMode == "first":
+            translations = -shifts[0, :]
+            ed = {"shiftsTriMat": shifts, "corrTriMat": corr, "originTriMat": orig, "peaksigTriMat": psig,
+                  "translations": translations.copy()}
+        else:
+            ed = hm.solve_shifts(shifts, corr, psig, shapeImage=[P0, P1], maxShift=reg.maxShift,
+                                 weightMode=reg.weightMode, peaksigThres=reg.peaksigThres, logisticK=reg.logisticK,
+                                 logisticNu=reg.logisticNu)
+            ed["originTriMat"] = orig
+            if reg.weightMode == "autologistic":
+                out["peaksigThres"] = ed["peaksigThres"]
+                out["logisticK"] = ed["logisticK"]
+                out["logisticNu"] = ed["logisticNu"]
+            translations = ed["translations"].copy()
+        edl.append(ed)
+        out["errorDictList"] = edl
+        bench["solve1"] = time.time()
+
+        # ---- shifts and sums (applyShifts zorro.py:1734-1808)
+        if reg.originMode == "centroid":
+            translations = translations - np.mean(translations, axis=0)
+        if not (reg.subPixReg > 1.0 and reg.shiftMethod == "lanczos"):
+            if reg.subPixReg > 1.0 and reg.shiftMethod == "fourier":
+                raise ValueError("shiftMethod 'fourier' is not supported by the GPU path")
+            # integer roll only (zorro.py:1790-1796)
+            params = [(int(v[0]), int(v[1]), 0, np.array([0, 1.0, 0]), np.array([0, 1.0, 0]))
+                      for v in np.round(translations).astype(int)]
+        else:
+            params = hm.shift_params(translations)
+        sh = (Shift * N)()
+        for n, (ry, rx, ap, ky, kx) in enumerate(params):
+            sh[n].roll_y, sh[n].roll_x, sh[n].apply = ry, rx, ap
+            for i in range(3):
+                sh[n].ky[i] = float(ky[i])
+                sh[n].kx[i] = float(kx[i])
+        sh_dev = torch.frombuffer(bytearray(bytes(sh)), dtype=torch.uint8).to(self.dev, non_blocking=True)
+        isum = self.tensor("isum", (H, W), torch.float32)
+        esum = self.tensor("esum", (H, W), torch.float32)
+        osum = self.tensor("osum", (H, W), torch.float32)
+        need_aligned = reg.keepAlignedImages or any(f in ("dose", "dosenorm") for f in filt)
+        aligned = self.tensor("aligned", (N, H, W), torch.float32) if need_aligned else None
+        self.call("G_shift_sum", "zr_shift_sum", C.byref(frames), sh_dev.data_ptr(), isum.data_ptr(), esum.data_ptr(),
+                  osum.data_ptr(), aligned.data_ptr() if aligned is not None else None, st)
+        bench["shifts1"] = time.time()
+
+        # ---- lazy FRC (zorro.py:2226-2310)
+        frc = frc2d = None
+        if reg.doEvenOddFRC:
+            raise ValueError("doEvenOddFRC (independent half-set FRC) is not supported by the GPU path yet")
+        if reg.doLazyFRC:
+            offs, tiles = hm.frc_tiles((H, W), translations)
+            box = 512
+            if len(offs) and (offs.min() < 0 or (offs[:, 0] + box).max() > H or (offs[:, 1] + box).max() > W):
+                raise ValueError("tiledFRC: tiles %s leave the %dx%d image (negative crop limits)" % (tiles, H, W))
+            if len(offs) == 0:
+                frc = np.full(box // 2, np.nan)
+                frc2d = np.full((box, box), np.nan, dtype=np.float32)
+            else:
+                offs_dev = torch.from_numpy(offs.reshape(-1)).to(self.dev, non_blocking=True)
+                nr = box // 2
+                fwb = self.lib.zr_frc_work_bytes(len(offs), box)
+                f2 = self.tensor("frc2d", (box, box), torch.float32)
+                fr = self.tensor("frc", (nr,), torch.float64)
+                self.call("H_frc", "zr_tiled_frc", esum.data_ptr(), osum.data_ptr(), H, W, box, offs_dev.data_ptr(), len(offs),
+                          f2.data_ptr(), fr.data_ptr(), nr, self.ptr("frcwork", fwb), fwb, st)
+                frc2d, frc = f2, fr
+        bench["frc1"] = time.time()
+
+        # ---- dose filter (zorro.py:2349-2494)
+        filt_sum = None
+        for fm in filt:
+            if fm in ("dose", "dosenorm"):
+                mean_sum = float(isum.double().mean().item()) if reg.doseFiltParam[0] is None else None
+                dc = hm.dose_constants(N, [P0, P1], reg.pixelsize, reg.voltage, reg.doseFiltParam, mean_sum)
+                dp = DoseParams(dc["A"], dc["B"], dc["C"], dc["order"], dc["vs"], dc["invPSx"], dc["invPSy"],
+                                int(fm == "dosenorm"))
+                tq = torch.from_numpy(dc["thresQ"].astype(np.float32)).to(self.dev, non_blocking=True)
+                de = torch.from_numpy(dc["dose_end"].astype(np.float32)).to(self.dev, non_blocking=True)
+                fixed = self.lib.zr_dose_work_bytes(P0, P1, 0)
+                perf = self.lib.zr_dose_work_bytes(P0, P1, 1) - fixed
+                nch = max(2, min(N + (N & 1), (DOSE_WORK - fixed) // perf))
+                dwb = fixed + nch * perf
+                filt_sum = self.tensor("filtsum", (H, W), torch.float32)
+                self.call("I_dose", "zr_dose_filter", aligned.data_ptr(), N, H, W, C.byref(dp), tq.data_ptr(), de.data_ptr(),
+                          P0, P1, filt_sum.data_ptr(), self.ptr("dosework", dwb), dwb, st)
+        bench["dose1"] = time.time()
+
+        # ---- results back to the host (or left on the device)
+        out["translations"] = translations
+        dev_out = bool(getattr(reg, "returnDeviceArrays", False))
+
+        def fetch(t):
+            if isinstance(t, np.ndarray):
+                return t
+            return t.clone() if dev_out else t.cpu().numpy().copy()
+
+        out["imageSum"] = fetch(isum)
+        if frc is not None:
+            out["FRC"] = fetch(frc)
+            out["FRC2D"] = fetch(frc2d)
+        if filt_sum is not None:
+            out["filtSum"] = fetch(filt_sum)
+        if reg.keepAlignedImages:
+            out["images"] = fetch(aligned)
+        out["hotpixInfo"] = hotinfo
+        out["shapeOriginal"] = [H, W]
+        out["masks"] = np.ones([1, H, W], dtype=bool) if not user_mask else reg.masks
+        bench["align1"] = time.time()
+        b = dict(reg.bench)
+        b.update(bench)
+        out["bench"] = b
+        return out
