@@ -29,8 +29,9 @@ absent or unbuildable here:
   ``scipy.optimize.basinhopping`` (``zorro.py:1415,1422``).  Here that call is
   answered by the exact optimum of the same objective (linear programme,
   HiGHS).  The logistic fit's basinhopping (``zorro.py:2008``) is answered by
-  the deterministic multi-start minimisation of the same objective and bounds
-  in ``oracle.zorro_oracle.logistic_fit_deterministic`` (basinhopping is
+  the deterministic Nelder-Mead minimisation of the same objective from the
+  same start point within the same bounds
+  (``oracle.zorro_oracle.logistic_fit_deterministic``) (basinhopping is
   chaotic here: 1e-9 changes of its input change the fit by O(1)).
 
 The float dtypes are switched to float64/complex128 after loading, the way
@@ -157,7 +158,8 @@ class _SolverShim:
     """Stands in for ``scipy.optimize`` inside the loaded reference module.
 
     ``basinhopping`` on the reference's shift objective is answered with the
-    exact weighted-L1 optimum; on the logistic objective it runs seeded."""
+    exact weighted-L1 optimum; on the logistic objective by a deterministic
+    minimisation (both from ``oracle.zorro_oracle``)."""
 
     def __init__(self, util):
         self._util = util
@@ -170,6 +172,7 @@ class _SolverShim:
         if func is self._util.weightedErrorNorm:
             A, b, w = mk["args"]
             bounds = mk["bounds"]
+            from oracle.zorro_oracle import weighted_l1_exact
             return types.SimpleNamespace(x=weighted_l1_exact(A, b, w, bounds))
         if func is self._util.minLogistic:
             from oracle.zorro_oracle import logistic_fit_deterministic
@@ -177,26 +180,6 @@ class _SolverShim:
             (lo, hi) = mk["bounds"][0]
             return types.SimpleNamespace(x=logistic_fit_deterministic(hSigma, cdf, lo, hi, x0[0]))
         raise RuntimeError("unexpected basinhopping objective %r" % func)
-
-
-def weighted_l1_exact(A, b, w, bounds):
-    """argmin_x sum(w*|A x - b|) within box bounds, as a linear programme.
-
-    Variables [x (n), t (m)]: minimise w.t subject to A x - t <= b and
-    -A x - t <= -b, t >= 0."""
-    A = np.asarray(A, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
-    w = np.asarray(w, dtype=np.float64)
-    m, n = A.shape
-    c = np.concatenate([np.zeros(n), w])
-    I = np.eye(m)
-    A_ub = np.block([[A, -I], [-A, -I]])
-    b_ub = np.concatenate([b, -b])
-    bnds = [tuple(map(float, bb)) for bb in np.asarray(bounds)] + [(0.0, None)] * m
-    res = scipy.optimize.linprog(c, A_ub=A_ub, b_ub=b_ub, bounds=bnds, method="highs")
-    if not res.success:
-        raise RuntimeError("weighted L1 LP failed: " + str(res.message))
-    return res.x[:n]
 
 
 _LOADED = {}

@@ -17,8 +17,8 @@ Parity: pinned against fixtures produced by running the unmodified reference
 are fixed where the reference is stochastic (its shift solve and logistic fit
 use unseeded ``scipy.optimize.basinhopping``): the shift solve returns the
 exact weighted-L1 optimum (linear programme, HiGHS) and the logistic fit is
-the deterministic multi-start search of ``logistic_fit_deterministic`` on the
-same objective and bounds.
+the deterministic Nelder-Mead minimisation of ``logistic_fit_deterministic``
+on the same objective, start point and bounds.
 """
 from __future__ import annotations
 
@@ -261,14 +261,26 @@ def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diag
 # --------------------------------------------------------------------------
 
 def weighted_l1_exact(A, b, w, bounds):
-    """argmin sum(w*|A x - b|) in a box, as an LP (HiGHS).  The reference's
-    objective is zorro_util.py:849-851."""
+    """argmin sum(w*|A x - b|) in a box (the objective of
+    zorro_util.py:849-851), exactly.  Solved as the dual linear programme
+    max b.y s.t. A^T y = 0, |y| <= w (HiGHS), whose equality multipliers are
+    the primal optimum; when that point leaves the box the bounded primal LP
+    is solved instead."""
+    A = np.asarray(A, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    w = np.asarray(w, dtype=np.float64)
     m, n = A.shape
-    c = np.concatenate([np.zeros(n), np.asarray(w, dtype=np.float64)])
+    bnd = np.asarray(bounds, dtype=np.float64)
+    res = scipy.optimize.linprog(-b, A_eq=A.T, b_eq=np.zeros(n), bounds=list(zip(-w, w)), method="highs")
+    if res.success:
+        x = -res.eqlin.marginals
+        if np.all(x >= bnd[:, 0]) and np.all(x <= bnd[:, 1]):
+            return x
+    c = np.concatenate([np.zeros(n), w])
     I = np.eye(m)
     A_ub = np.block([[A, -I], [-A, -I]])
     b_ub = np.concatenate([b, -b])
-    bnds = [tuple(map(float, bb)) for bb in np.asarray(bounds)] + [(0.0, None)] * m
+    bnds = [tuple(map(float, bb)) for bb in bnd] + [(0.0, None)] * m
     res = scipy.optimize.linprog(c, A_ub=A_ub, b_ub=b_ub, bounds=bnds, method="highs")
     if not res.success:
         raise RuntimeError("weighted L1 LP failed: " + str(res.message))
@@ -283,26 +295,23 @@ def min_logistic(x, hSigma, cdf):
 
 def _logistic_cdf_error64(x, hSigma, cdf):
     """min_logistic without its final float32 cast (zorro_util.py:862-863)."""
-    return np.sum(np.abs(cdf - (1.0 - 1.0 / (1.0 + np.exp(-x[1] * (-hSigma + x[0]))) ** x[2])))
+    with np.errstate(over="ignore"):
+        return np.sum(np.abs(cdf - (1.0 - 1.0 / (1.0 + np.exp(-x[1] * (-hSigma + x[0]))) ** x[2])))
 
 
 def logistic_fit_deterministic(hSigma, cdf, lo, hi, mean):
-    """The global minimum of the reference's logistic-CDF error within its
-    bounds (zorro.py:2000-2008), found deterministically: L-BFGS-B from the
-    reference's start point and 27 fixed others, best value wins (earliest
-    start on ties within 1e-9).  The reference's unseeded basinhopping returns
-    a different point every run and jumps between near-equal minima under
-    1e-9 perturbations of its input; this search does not."""
+    """A deterministic minimiser of the reference's logistic-CDF error within
+    its bounds (zorro.py:2000-2008): Nelder-Mead from the reference's start
+    point (mean, 5, 1), to tight tolerances.  The reference's unseeded
+    basinhopping returns a different point every run and jumps between
+    near-equal minima under 1e-9 perturbations of its input; this minimiser
+    repeats and moves continuously with its input."""
     bounds = ((lo, hi), (0.1, 20.0), (0.05, 5.0))
-    starts = [(mean, 5.0, 1.0)] + [(lo + f * (hi - lo), K, nu) for f in (0.25, 0.5, 0.75)
-                                   for K in (1.0, 5.0, 12.0) for nu in (0.3, 1.0, 3.0)]
-    best = None
-    for x0 in starts:
-        r = scipy.optimize.minimize(_logistic_cdf_error64, x0, args=(hSigma, cdf), method="L-BFGS-B", bounds=bounds,
-                                    options={"ftol": 1e-15, "gtol": 1e-12, "maxiter": 1000})
-        if best is None or r.fun < best.fun * (1.0 - 1e-9):
-            best = r
-    return best.x
+    with np.errstate(over="ignore"):
+        r = scipy.optimize.minimize(_logistic_cdf_error64, (mean, 5.0, 1.0), args=(hSigma, cdf), method="Nelder-Mead",
+                                    bounds=bounds, options={"xatol": 1e-10, "fatol": 1e-14, "maxiter": 4000,
+                                                            "maxfev": 8000})
+    return r.x
 
 
 def cdf_logistic_curve(peaksigTriMat, seed=LOGISTIC_SEED):

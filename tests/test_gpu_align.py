@@ -194,5 +194,10 @@ def test_golden_fixtures():
         if same_traj and "FRC" in g and not np.all(np.isnan(g["FRC"])):
             assert np.nanmax(np.abs(reg.FRC - g["FRC"])) <= FRC_TOL, name
         if "hot_guessHotpix" in g:
+            # exact against the oracle on this platform; the fixture was made on
+            # another NumPy/SciPy build, whose normal-CDF fit (L-BFGS-B) can
+            # move a pixel sitting on the cut-off
+            ref = zo.align_image_stack(mv["images"], **attrs)
             for k in ("guessDeadpix", "guessHotpix", "neighborPix"):
-                assert reg.hotpixInfo[k] == int(g["hot_" + k]), (name, k)
+                assert reg.hotpixInfo[k] == ref["hotpixInfo"][k], (name, k)
+                assert abs(reg.hotpixInfo[k] - int(g["hot_" + k])) <= 1 + 0.01 * int(g["hot_" + k]), (name, k)

@@ -17,6 +17,7 @@
 namespace zr {
 
 constexpr int FRC_NB = 4;
+constexpr int FRC_TPG = 8;  // tiles accumulated per CTA of the column pass
 
 // Hann window of apodization('hann', box): radius box/2, circular.
 __device__ __forceinline__ float hann_at(int y, int x, int B) {
@@ -67,10 +68,12 @@ __global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB))
   constexpr int PER = (B * FRC_NB + T - 1) / T;
   extern __shared__ float2 sm[];
   const int k0 = blockIdx.x * FRC_NB;
+  const int t0 = blockIdx.y * FRC_TPG;
+  const int t1 = min(n_tiles, t0 + FRC_TPG);
   double acc[PER];
 #pragma unroll
   for (int i = 0; i < PER; i++) acc[i] = 0.0;
-  for (int t = 0; t < n_tiles; t++) {
+  for (int t = t0; t < t1; t++) {
     const size_t tb = (size_t)t * (B / FRC_NB) * K4 * FRC_NB;
     for (int e = threadIdx.x; e < B * FRC_NB; e += T) {
       const int gg = e / (FRC_NB * FRC_NB), j = e - gg * (FRC_NB * FRC_NB);
@@ -100,25 +103,27 @@ __global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB))
     const int e = threadIdx.x + i * T;
     if (e < B * FRC_NB) {
       const int c = e / B, y = e - c * B;
-      half[(size_t)y * K4 + k0 + c] = acc[i];
+      half[((size_t)blockIdx.y * B + y) * K4 + k0 + c] = acc[i];
     }
   }
 }
 
 // fftshift + DC normalisation into frc2d, and per-block ring partial sums.
-__global__ void k_frc_assemble(const double* __restrict__ half, int B, int K4, int nr, float* __restrict__ frc2d,
-                               double* __restrict__ part) {
+__global__ void k_frc_assemble(const double* __restrict__ half, int ngroups, int B, int K4, int nr,
+                               float* __restrict__ frc2d, double* __restrict__ part) {
   extern __shared__ double rs[];  // [2][nr]
   for (int i = threadIdx.x; i < 2 * nr; i += blockDim.x) rs[i] = 0.0;
   __syncthreads();
-  const double dc = half[0];
+  const size_t plane = (size_t)B * K4;
+  double dc = 0.0;
+  for (int g = 0; g < ngroups; g++) dc += half[g * plane];
   const int hb = B / 2;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < B * B; p += gridDim.x * blockDim.x) {
     const int i = p / B, j = p - i * B;
     const int ky = (i + hb) & (B - 1), kx = (j + hb) & (B - 1);
-    double v;
-    if (kx <= hb) v = half[(size_t)ky * K4 + kx];
-    else v = half[(size_t)((B - ky) & (B - 1)) * K4 + (B - kx)];
+    const size_t q = (kx <= hb) ? (size_t)ky * K4 + kx : (size_t)((B - ky) & (B - 1)) * K4 + (B - kx);
+    double v = 0.0;
+    for (int g = 0; g < ngroups; g++) v += half[g * plane + q];
     v = v / dc;
     frc2d[p] = (float)v;
     const double xx = j - hb, yy = i - hb;
@@ -156,8 +161,9 @@ static int run_frc(const float* even, const float* odd, int W, const int* offs, 
   const int K4 = zr_spectrum_pitch(B);
   float2* RE = (float2*)work;
   float2* RO = RE + (size_t)n_tiles * B * K4;
+  const int ngroups = (n_tiles + FRC_TPG - 1) / FRC_TPG;
   double* half = (double*)(RO + (size_t)n_tiles * B * K4);
-  double* part = half + (size_t)B * K4;
+  double* part = half + (size_t)ngroups * B * K4;
   {
     constexpr int T = fft_threads(B, FRC_NB);
     const size_t smem = (size_t)FRC_NB * ld_of(B) * sizeof(float2);
@@ -169,10 +175,10 @@ static int run_frc(const float* even, const float* odd, int W, const int* offs, 
     constexpr int T = fft_threads(B, 2 * FRC_NB);
     const size_t smem = (size_t)2 * FRC_NB * ld_of(B) * sizeof(float2);
     ZR_TRY(cuda_check(cudaFuncSetAttribute(k_frc_cols<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "frc attr"));
-    k_frc_cols<B><<<K4 / FRC_NB, T, smem, st>>>(RE, RO, n_tiles, K4, half, tw);
+    k_frc_cols<B><<<dim3(K4 / FRC_NB, ngroups), T, smem, st>>>(RE, RO, n_tiles, K4, half, tw);
     ZR_TRY(launched("k_frc_cols"));
   }
-  k_frc_assemble<<<FRC_ASM_BLOCKS, 512, 2 * nr * sizeof(double), st>>>(half, B, K4, nr, frc2d, part);
+  k_frc_assemble<<<FRC_ASM_BLOCKS, 512, 2 * nr * sizeof(double), st>>>(half, ngroups, B, K4, nr, frc2d, part);
   ZR_TRY(launched("k_frc_assemble"));
   k_frc_rings<<<1, 512, 0, st>>>(part, FRC_ASM_BLOCKS, nr, nout, frc);
   return launched("k_frc_rings");
@@ -185,7 +191,8 @@ using namespace zr;
 extern "C" size_t zr_frc_work_bytes(int n_tiles, int box) {
   const size_t K4 = zr_spectrum_pitch(box);
   const int nr = (int)ceil(sqrt((double)(box / 2) * (box / 2) * 2.0)) + 1;
-  return 2 * (size_t)n_tiles * box * K4 * sizeof(float2) + (size_t)box * K4 * sizeof(double) +
+  const size_t ngroups = (n_tiles + FRC_TPG - 1) / FRC_TPG;
+  return 2 * (size_t)n_tiles * box * K4 * sizeof(float2) + ngroups * box * K4 * sizeof(double) +
          (size_t)FRC_ASM_BLOCKS * 2 * (nr + 1) * sizeof(double);
 }
 

@@ -59,12 +59,8 @@ __device__ int gauss_weights(double sigma, float* w) {
   if (threadIdx.x == 0) {
     const double c = -0.5 / (sigma * sigma);
     double s = 0.0;
-    double tmp[2 * PK_MAXR + 1];
-    for (int k = -r; k <= r; k++) {
-      tmp[k + r] = exp(c * (double)k * (double)k);
-      s += tmp[k + r];
-    }
-    for (int k = 0; k <= 2 * r; k++) w[k] = (float)(tmp[k] / s);
+    for (int k = -r; k <= r; k++) s += exp(c * (double)k * (double)k);
+    for (int k = -r; k <= r; k++) w[k + r] = (float)(exp(c * (double)k * (double)k) / s);
   }
   return r;
 }
@@ -128,53 +124,68 @@ struct FiltStats {
   int n;
 };
 
+constexpr int PK_TX = 64;            // column lanes of the filter passes
+constexpr int PK_TY = PK_T / PK_TX;  // rows per block (== PK_RB)
+static_assert(PK_TY == PK_RB, "row block must match the thread layout");
+
 // Visit every filtered value of the window.  MODE 0: statistics of all
-// values.  MODE 1: masked statistics plus argmax of (mask ? f : 0).
+// values.  MODE 1: masked statistics plus argmax of (mask ? f : 0).  rtab[i +
+// PK_MAXR] is the 'reflect' index of i for i in [-PK_MAXR, w + PK_MAXR).
 template <int MODE>
-__device__ void filter_pass(const float* C, float* V, int w, int mS, int ry, int rx, const float* wy,
-                            const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st,
+__device__ void filter_pass(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx,
+                            const float* wy, const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st,
                             float& amax, int& aidx) {
+  const int tx = threadIdx.x & (PK_TX - 1), ty = threadIdx.x / PK_TX;
   float s1 = 0.0f, s2 = 0.0f, mx = -INFINITY;
   float bv = -INFINITY;
   int bi = 0x7fffffff;
   int cnt = 0;
   for (int y0 = 0; y0 < w; y0 += PK_RB) {
-    const int nr = (w - y0) < PK_RB ? (w - y0) : PK_RB;
-    for (int e = threadIdx.x; e < nr * w; e += PK_T) {
-      const int i = e / w, x = e - i * w;
-      const int y = y0 + i;
-      float acc = 0.0f;
-      if (ry == 0) {
-        acc = C[y * w + x];
-      } else {
-        for (int k = -ry; k <= ry; k++) acc = fmaf(wy[k + ry], C[reflect_idx(y + k, w) * w + x], acc);
+    const int y = y0 + ty;
+    if (y < w) {
+      for (int x = tx; x < w; x += PK_TX) {
+        float acc = 0.0f;
+        if (ry == 0) {
+          acc = C[y * w + x];
+        } else if (y >= ry && y + ry < w) {
+          const float* p = C + (y - ry) * w + x;
+          for (int k = 0; k <= 2 * ry; k++) acc = fmaf(wy[k], p[k * w], acc);
+        } else {
+          const int* rt = rtab + PK_MAXR + y - ry;
+          for (int k = 0; k <= 2 * ry; k++) acc = fmaf(wy[k], C[rt[k] * w + x], acc);
+        }
+        V[ty * w + x] = acc;
       }
-      V[i * w + x] = acc;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < nr * w; e += PK_T) {
-      const int i = e / w, x = e - i * w;
-      float f = 0.0f;
-      if (rx == 0) {
-        f = V[i * w + x];
-      } else {
-        for (int k = -rx; k <= rx; k++) f = fmaf(wx[k + rx], V[i * w + reflect_idx(x + k, w)], f);
-      }
-      const int y = y0 + i;
-      bool in = true;
-      if (MODE == 1) {
-        const int dy = y - mS, dx = x - mS;
-        in = !use_mask || (dy * dy + dx * dx < mS * mS);
-        const float mv = in ? f : 0.0f;
-        const int idx = y * w + x;
-        if (mv > bv || (mv == bv && idx < bi)) { bv = mv; bi = idx; }
-      }
-      if (in) {
-        const float d = f - c;
-        s1 += d;
-        s2 = fmaf(d, d, s2);
-        mx = fmaxf(mx, f);
-        cnt++;
+    if (y < w) {
+      const float* vr = V + ty * w;
+      for (int x = tx; x < w; x += PK_TX) {
+        float f = 0.0f;
+        if (rx == 0) {
+          f = vr[x];
+        } else if (x >= rx && x + rx < w) {
+          const float* p = vr + x - rx;
+          for (int k = 0; k <= 2 * rx; k++) f = fmaf(wx[k], p[k], f);
+        } else {
+          const int* rt = rtab + PK_MAXR + x - rx;
+          for (int k = 0; k <= 2 * rx; k++) f = fmaf(wx[k], vr[rt[k]], f);
+        }
+        bool in = true;
+        if (MODE == 1) {
+          const int dy = y - mS, dx = x - mS;
+          in = !use_mask || (dy * dy + dx * dx < mS * mS);
+          const float mv = in ? f : 0.0f;
+          const int idx = y * w + x;
+          if (mv > bv || (mv == bv && idx < bi)) { bv = mv; bi = idx; }
+        }
+        if (in) {
+          const float d = f - c;
+          s1 += d;
+          s2 = fmaf(d, d, s2);
+          mx = fmaxf(mx, f);
+          cnt++;
+        }
       }
     }
     __syncthreads();
@@ -194,13 +205,14 @@ __device__ void filter_pass(const float* C, float* V, int w, int mS, int ry, int
   }
 }
 
-__device__ double objective(const float* C, float* V, int w, int mS, double sigma, float c, PkShared& sh) {
+__device__ double objective(const float* C, float* V, const int* rtab, int w, int mS, double sigma, float c,
+                            PkShared& sh) {
   const int r = gauss_weights(sigma, sh.wy);
   __syncthreads();
   FiltStats st;
   float am;
   int ai;
-  filter_pass<0>(C, V, w, mS, r, r, sh.wy, sh.wy, c, sh, false, st, am, ai);
+  filter_pass<0>(C, V, rtab, w, mS, r, r, sh.wy, sh.wy, c, sh, false, st, am, ai);
   const double n = (double)st.n;
   const double m1 = st.s1 / n;
   const double var = st.s2 / n - m1 * m1;
@@ -212,8 +224,8 @@ __device__ __forceinline__ double sgn1(double v) { return v > 0.0 ? 1.0 : (v < 0
 
 // Bounded Brent minimisation (FMM FMIN).  Returns the abscissa of the best
 // value; *nfev receives the number of function values.
-__device__ double fmin_bounded(const float* C, float* V, int w, int mS, float c, PkShared& sh, double lo,
-                               double hi, double xatol, int maxfun, int* nfev) {
+__device__ double fmin_bounded(const float* C, float* V, const int* rtab, int w, int mS, float c, PkShared& sh,
+                               double lo, double hi, double xatol, int maxfun, int* nfev) {
   const double sqrt_eps = sqrt(2.2e-16);
   const double golden = 0.5 * (3.0 - sqrt(5.0));
   double a = lo, b = hi;
@@ -221,7 +233,7 @@ __device__ double fmin_bounded(const float* C, float* V, int w, int mS, float c,
   double nfc = fulc, xf = fulc;
   double rat = 0.0, e = 0.0;
   double x = xf;
-  double fx = objective(C, V, w, mS, x, c, sh);
+  double fx = objective(C, V, rtab, w, mS, x, c, sh);
   int num = 1;
   double ffulc = fx, fnfc = fx;
   double xm = 0.5 * (a + b);
@@ -252,7 +264,7 @@ __device__ double fmin_bounded(const float* C, float* V, int w, int mS, float c,
       rat = golden * e;
     }
     x = xf + sgn1(rat) * fmax(fabs(rat), tol1);
-    const double fu = objective(C, V, w, mS, x, c, sh);
+    const double fu = objective(C, V, rtab, w, mS, x, c, sh);
     num += 1;
     if (fu <= fx) {
       if (x >= xf) a = xf; else b = xf;
@@ -291,17 +303,19 @@ __device__ float filtered_at(const float* C, int w, int y, int x, int ry, int rx
   return f;
 }
 
-__global__ void __launch_bounds__(PK_T) k_peaks(const float* __restrict__ cwin, int mS, zr_peak_params_t p,
+__global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwin, int mS, zr_peak_params_t p,
                                                zr_peak_result_t* __restrict__ res, const float2* __restrict__ tw) {
   extern __shared__ float smf[];
   __shared__ PkShared sh;
   __shared__ float2 patchF[16 * 16];
+  __shared__ int rtab[2 * PK_MAXR + 2 * 112];
   const int w = 2 * mS;
   const int w2 = w * w;
   float* C = smf;
   float* V = smf + w2;
   const float* src = cwin + (size_t)blockIdx.x * w2;
   for (int e = threadIdx.x; e < w2; e += PK_T) C[e] = src[e];
+  for (int i = threadIdx.x; i < w + 2 * PK_MAXR; i += PK_T) rtab[i] = reflect_idx(i - PK_MAXR, w);
   __syncthreads();
   const float origin = C[mS * w + mS];
   if (p.suppress_origin) {
@@ -328,7 +342,7 @@ __global__ void __launch_bounds__(PK_T) k_peaks(const float* __restrict__ cwin, 
   double sigy = 0.0, sigx = 0.0, sig_opt = nan("");
   int nfev = 0;
   if (p.bmode == 1) {
-    sig_opt = fmin_bounded(C, V, w, mS, c, sh, p.opti_lo, p.opti_hi, p.opti_xatol, p.opti_maxiter, &nfev);
+    sig_opt = fmin_bounded(C, V, rtab, w, mS, c, sh, p.opti_lo, p.opti_hi, p.opti_xatol, p.opti_maxiter, &nfev);
     sigy = sigx = sig_opt;
   } else if (p.bmode == 2) {
     sigy = p.conv_sigma_y;
@@ -340,7 +354,7 @@ __global__ void __launch_bounds__(PK_T) k_peaks(const float* __restrict__ cwin, 
   FiltStats st;
   float amax = 0.0f;
   int aidx = 0;
-  filter_pass<1>(C, V, w, mS, ry, rx, sh.wy, sh.wx, c, sh, p.use_mask != 0, st, amax, aidx);
+  filter_pass<1>(C, V, rtab, w, mS, ry, rx, sh.wy, sh.wx, c, sh, p.use_mask != 0, st, amax, aidx);
   const int cy = aidx / w, cx = aidx - (aidx / w) * w;
   double peaksig = nan("");
   {

@@ -26,8 +26,10 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR))
   constexpr int T = fft_threads(P1, NBR);
   constexpr int LD = ld_of(P1);
   extern __shared__ float2 sm[];
-  const int g = blockIdx.x;
-  const int nl = blockIdx.y;
+  // frames vary fastest so that concurrent CTAs read the same rows of the
+  // gain and hot-pixel maps through L2
+  const int g = blockIdx.y;
+  const int nl = blockIdx.x;
   const int n = frame0 + nl;
   float mu = 0.0f;
   if (mode == 0 && mean_sub) mu = (float)(mean_sub[n] * inv_area);
@@ -130,7 +132,7 @@ static int launch_rows(const FrameSrc& f, const float* mask, const double* mean_
   const size_t smem = (size_t)NBR * ld_of(P) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_rows<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_fwd_rows attr"));
-  k_fwd_rows<P><<<dim3(H4, nfr), T, smem, st>>>(f, mask, mean_sub, inv_area, frame0, mode, rows, cols, C1, K4,
+  k_fwd_rows<P><<<dim3(nfr, H4), T, smem, st>>>(f, mask, mean_sub, inv_area, frame0, mode, rows, cols, C1, K4,
                                                  H4, RU, RV, tw);
   return launched("k_fwd_rows");
 }

@@ -60,8 +60,10 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC))
   constexpr int T = fft_threads(C0, XC_NBC);
   constexpr int LD = ld_of(C0);
   extern __shared__ float2 sm[];
-  const int k0 = blockIdx.x * XC_NBC;
-  const int jl = blockIdx.y;
+  // jobs vary fastest across the grid so that the CTAs resident at one time
+  // share the same column tile of every spectrum through L2
+  const int k0 = blockIdx.y * XC_NBC;
+  const int jl = blockIdx.x;
   const float2 *A, *B;
   job_operands(J, J.job0 + jl, A, B);
   const int half = C1 / 2, hc = C0 / 2;
@@ -156,7 +158,7 @@ static int launch_xc_cols(const XcJobs& J, int nj, int C1, int K4, int mS, float
   const size_t smem = (size_t)XC_NBC * ld_of(C0) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_xc_cols attr"));
-  k_xc_cols<C0><<<dim3(K4 / XC_NBC, nj), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
+  k_xc_cols<C0><<<dim3(nj, K4 / XC_NBC), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
   return launched("k_xc_cols");
 }
 

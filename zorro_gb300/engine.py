@@ -234,8 +234,13 @@ class Engine:
         msub = None
         if reg.subtractFrameMean and not user_mask:
             msub = self.tensor("msub", (N,), torch.float64)
-            msub.zero_()
-            self.call("C_spectra", "zr_frame_sums", C.byref(frames), msub.data_ptr(), st)
+            if "hot" in filt:
+                # any per-frame constant is exact; the mean frame of the unaligned
+                # sum is close to every frame's mean and costs no extra pass
+                msub.copy_(tot[0].expand(N) / N)
+            else:
+                msub.zero_()
+                self.call("C_spectra", "zr_frame_sums", C.byref(frames), msub.data_ptr(), st)
 
         # ---- spectra (xcorrnm2_tri zorro.py:814-925)
         bench["xcorr0"] = time.time()

@@ -17,7 +17,7 @@ import scipy.stats
 # The reference's logistic fit and drift solve call the stochastic
 # scipy.optimize.basinhopping without a seed (zorro.py:1415,1422,2008).  Here
 # the drift solve is the exact weighted-L1 optimum of the same objective and
-# the logistic fit a deterministic multi-start search, so results repeat.
+# the logistic fit a deterministic Nelder-Mead search, so results repeat.
 
 
 def tri_indices(N, triMode="diag", diagWidth=5, diagStart=0):
@@ -65,9 +65,18 @@ def equation_matrix(tri):
 
 def l1_solve(A, b, w, lo, hi):
     """argmin_x sum(w * |A x - b|) with lo <= x <= hi (the objective of
-    zorro_util.py:849-851), exactly, as a linear programme."""
+    zorro_util.py:849-851), exactly.  The dual linear programme
+    (max b.y s.t. A^T y = 0, |y| <= w) has only n equality rows; its
+    equality multipliers are the primal optimum.  If that point leaves the
+    box, the bounded primal LP is solved instead."""
     m, n = A.shape
-    cost = np.concatenate([np.zeros(n), np.asarray(w, dtype=np.float64)])
+    w = np.asarray(w, dtype=np.float64)
+    res = scipy.optimize.linprog(-b, A_eq=A.T, b_eq=np.zeros(n), bounds=list(zip(-w, w)), method="highs")
+    if res.success:
+        x = -res.eqlin.marginals
+        if np.all(x >= lo) and np.all(x <= hi):
+            return x
+    cost = np.concatenate([np.zeros(n), w])
     eye = np.eye(m)
     A_ub = np.block([[A, -eye], [-A, -eye]])
     b_ub = np.concatenate([b, -b])
@@ -80,7 +89,8 @@ def l1_solve(A, b, w, lo, hi):
 
 def _logistic_cdf_error(x, hSigma, cdf):
     """The logistic-CDF error of zorro_util.py:862-863 (float64)."""
-    model = 1.0 - 1.0 / (1.0 + np.exp(-x[1] * (-hSigma + x[0]))) ** x[2]
+    with np.errstate(over="ignore"):
+        model = 1.0 - 1.0 / (1.0 + np.exp(-x[1] * (-hSigma + x[0]))) ** x[2]
     return np.sum(np.abs(cdf - model))
 
 
@@ -89,10 +99,9 @@ def logistic_fit(peaksigTriMat):
 
     The reference minimises the error with unseeded basinhopping, which
     returns a different point on every run.  Here the same objective is
-    minimised within the same bounds by L-BFGS-B from the reference's start
-    point and 27 fixed others; the best value wins (the earliest start on
-    ties within 1e-9), so the fit repeats and moves continuously with its
-    input."""
+    minimised from the reference's start point (mean, 5, 1) within the same
+    bounds by Nelder-Mead to tight tolerances, so the fit repeats and moves
+    continuously with its input."""
     ps = peaksigTriMat[peaksigTriMat > 0.0]
     bins = int(ps.size / 7.0)
     if bins <= 0:
@@ -102,17 +111,11 @@ def logistic_fit(peaksigTriMat):
     pdf = pdf.astype("float32")
     cdf = np.cumsum(pdf)
     cdf /= cdf[-1]
-    lo, hi = np.min(ps), np.max(ps)
-    bounds = ((lo, hi), (0.1, 20.0), (0.05, 5.0))
-    starts = [(np.mean(ps), 5.0, 1.0)] + [(lo + f * (hi - lo), K, nu) for f in (0.25, 0.5, 0.75)
-                                         for K in (1.0, 5.0, 12.0) for nu in (0.3, 1.0, 3.0)]
-    best = None
-    for x0 in starts:
-        r = scipy.optimize.minimize(_logistic_cdf_error, x0, args=(hSigma, cdf), method="L-BFGS-B", bounds=bounds,
-                                    options={"ftol": 1e-15, "gtol": 1e-12, "maxiter": 1000})
-        if best is None or r.fun < best.fun * (1.0 - 1e-9):
-            best = r
-    x = best.x
+    bounds = ((np.min(ps), np.max(ps)), (0.1, 20.0), (0.05, 5.0))
+    r = scipy.optimize.minimize(_logistic_cdf_error, (np.mean(ps), 5.0, 1.0), args=(hSigma, cdf), method="Nelder-Mead",
+                                bounds=bounds, options={"xatol": 1e-10, "fatol": 1e-14, "maxiter": 4000,
+                                                        "maxfev": 8000})
+    x = r.x
     return {"peaksigThres": x[0], "logisticK": x[1], "logisticNu": x[2], "pdfPeaks": pdf, "cdfPeaks": cdf,
             "hSigma": hSigma}
 
