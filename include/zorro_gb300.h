@@ -14,10 +14,11 @@
  *
  * Layouts (row-major, C order):
  *   frames      [N][H][W] raw counts (see zr_frames_t)
- *   spectrum    [C0+1][K4] complex float, K4 = zr_spectrum_pitch(C1): rows 0..C0-1
- *               are the Fourier-cropped frequencies ky in FFT order (row C0/2 holds
- *               ky = -C0/2), row C0 holds ky = +C0/2; column k holds kx = k for
- *               0 <= k <= C1/2 (the half-plane of a real image).
+ *   spectrum    [K4][C0+4] complex float, column-major: K4 = zr_spectrum_pitch(C1)
+ *               columns, column k holding kx = k for 0 <= k <= C1/2 (the half-plane
+ *               of a real image); in each column, elements 0..C0-1 are the
+ *               Fourier-cropped frequencies ky in FFT order (element C0/2 holds
+ *               ky = -C0/2), element C0 holds ky = +C0/2, the rest is padding.
  *   window      [w][w] float, w = 2*max_shift; element (a, b) is the correlation
  *               at shift (y, x) = (a - max_shift, b - max_shift).
  */
@@ -88,9 +89,10 @@ typedef struct zr_peak_result {
 } zr_peak_result_t;
 
 /* Per-frame shift applied by applyShifts (zorro.py:1774 ->
- * zorro_util.py:341-379): np.roll by (roll_y, roll_x), then the separable
- * 3x3 Lanczos kernel ky (x) kx with reflect boundaries (identity when
- * apply == 0). */
+ * zorro_util.py:341-379): np.roll by (roll_y, roll_x), given reduced modulo
+ * the frame height and width (0 <= roll_y < H, 0 <= roll_x < W), then the
+ * separable 3x3 Lanczos kernel ky (x) kx with reflect boundaries (identity
+ * when apply == 0). */
 typedef struct zr_shift {
   int roll_y, roll_x;
   int apply;

@@ -57,13 +57,14 @@ def spectra(images, P, C_, mean_sub=True):
               C_[0], C_[1], G.data_ptr(), S.data_ptr(), work.data_ptr(), wb, stream())
     torch.cuda.synchronize()
 
-    def cx(t, shape):
+    def cx(t, n):
+        # column-major [K4][C0+4] -> [C0+1][K4]
         a = t.cpu().numpy().astype(np.float64)
-        return (a[..., 0] + 1j * a[..., 1]).reshape(shape)
+        a = (a[..., 0] + 1j * a[..., 1]).reshape(n, K4, C_[0] + 4)[:, :, :C_[0] + 1]
+        return np.swapaxes(a, 1, 2)
 
     means = (msub.cpu().numpy() / (H * W)) if msub is not None else np.zeros(N)
-    return (cx(G, (N, C_[0] + 1, K4)), cx(S, (N, C_[0] + 1, K4)), cx(GM, (C_[0] + 1, K4)), means,
-            (G, S, GM))
+    return (cx(G, N), cx(S, N), cx(GM, 1)[0], means, (G, S, GM))
 
 
 def windows(dev_spectra, N, C_, mS, pairs):

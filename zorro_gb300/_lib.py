@@ -100,7 +100,7 @@ def load(path=None):
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("ZORRO_GB300_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise ZorroError("libzorrogb.so not found at %s: build it with `python -m zorro_gb300.build` "
                          "(there is no CPU fallback)" % path)

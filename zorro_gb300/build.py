@@ -50,14 +50,18 @@ def up_to_date():
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    if not force and up_to_date():
+def build(force=False, verbose=False, extra_flags=(), out=None, build_dir=None):
+    """Compile every csrc/*.cu and link ``out`` (default: the in-tree
+    libzorrogb.so).  ``extra_flags`` go to every nvcc compile."""
+    if out is None and not force and not extra_flags and up_to_date():
         return LIB
+    lib_path = out or LIB
+    bdir = build_dir or BUILD_DIR
     nvcc = nvcc_path()
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    os.makedirs(bdir, exist_ok=True)
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(bdir, os.path.basename(src)[:-3] + ".o")
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra_flags, "-I", INCLUDE, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -69,13 +73,13 @@ def build(force=False, verbose=False, extra_flags=()):
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

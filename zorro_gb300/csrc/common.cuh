@@ -59,6 +59,45 @@ __device__ __forceinline__ float load_corrected(const FrameSrc& f, int n, int y,
   return v;
 }
 
+// Corrected values of the four consecutive pixels p..p+3 (flattened within
+// the frame) of frame n.  Needs p % 4 == 0 and fstride % 4 == 0 (aligned
+// vector loads of every array).
+__device__ __forceinline__ float4 load4_corrected(const FrameSrc& f, int n, long long p) {
+  const long long i = (long long)n * f.fstride + p;
+  float4 v;
+  switch (f.type) {
+    case ZR_U8: {
+      const uchar4 r = __ldg(reinterpret_cast<const uchar4*>((const uint8_t*)f.raw + i));
+      v = make_float4(r.x, r.y, r.z, r.w);
+      break;
+    }
+    case ZR_U16: {
+      const ushort4 r = __ldg(reinterpret_cast<const ushort4*>((const uint16_t*)f.raw + i));
+      v = make_float4(r.x, r.y, r.z, r.w);
+      break;
+    }
+    case ZR_F16: {
+      const __half* h = (const __half*)f.raw + i;
+      const __half2 a = __ldg(reinterpret_cast<const __half2*>(h)), b = __ldg(reinterpret_cast<const __half2*>(h + 2));
+      v = make_float4(__low2float(a), __high2float(a), __low2float(b), __high2float(b));
+      break;
+    }
+    default: v = __ldg(reinterpret_cast<const float4*>((const float*)f.raw + i));
+  }
+  if (f.gain) {
+    const float4 g = __ldg(reinterpret_cast<const float4*>(f.gain + p));
+    v = make_float4(__fmul_rn(g.x, v.x), __fmul_rn(g.y, v.y), __fmul_rn(g.z, v.z), __fmul_rn(g.w, v.w));
+  }
+  if (f.gdiv != 0.0f)
+    v = make_float4(__fdiv_rn(v.x, f.gdiv), __fdiv_rn(v.y, f.gdiv), __fdiv_rn(v.z, f.gdiv), __fdiv_rn(v.w, f.gdiv));
+  if (f.ha) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(f.ha + p)), b = __ldg(reinterpret_cast<const float4*>(f.hb + p));
+    v = make_float4(__fmaf_rn(a.x, v.x, b.x), __fmaf_rn(a.y, v.y, b.y), __fmaf_rn(a.z, v.z, b.z),
+                    __fmaf_rn(a.w, v.w, b.w));
+  }
+  return v;
+}
+
 __device__ __forceinline__ int ilog2c(int v) { return 31 - __clz(v); }
 
 }  // namespace zr

@@ -19,7 +19,7 @@
 namespace zr {
 
 constexpr int DS_NBR = 4;  // rows per CTA (forward row pass)
-constexpr int DS_NBC = 2;  // columns per CTA (accumulating column pass)
+
 
 __device__ __forceinline__ int sym_idx(int i, int n) {
   int m = i % (2 * n);
@@ -27,7 +27,7 @@ __device__ __forceinline__ int sym_idx(int i, int n) {
 }
 
 template <int P1>
-__global__ void __launch_bounds__(fft_threads(P1, DS_NBR))
+__global__ void __launch_bounds__(fft_threads(P1, DS_NBR), fft_minblocks(P1))
     k_dose_rows(const float* __restrict__ img, int N, int H, int W, int f0, int K4, int P0,
                 float2* __restrict__ RW, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(P1, DS_NBR);
@@ -38,7 +38,9 @@ __global__ void __launch_bounds__(fft_threads(P1, DS_NBR))
   const int na = f0 + 2 * pl, nb = na + 1;
   for (int e = threadIdx.x; e < DS_NBR * P1; e += T) {
     const int r = e / P1, x = e - r * P1;
-    const int ys = sym_idx(g * DS_NBR + r, H), xs = sym_idx(x, W);
+    const int yy = g * DS_NBR + r;
+    const int ys = yy < H ? yy : (yy < 2 * H ? 2 * H - 1 - yy : sym_idx(yy, H));
+    const int xs = x < W ? x : (x < 2 * W ? 2 * W - 1 - x : sym_idx(x, W));
     const size_t p = (size_t)ys * W + xs;
     const float a = img[(size_t)na * H * W + p];
     const float b = nb < N ? img[(size_t)nb * H * W + p] : 0.0f;
@@ -46,12 +48,12 @@ __global__ void __launch_bounds__(fft_threads(P1, DS_NBR))
   }
   __syncthreads();
   block_fft<P1, DS_NBR, T, -1>(sm, tw);
-  const size_t H4 = P0 / DS_NBR;
-  const size_t fa = (size_t)(2 * pl) * H4 * K4 * DS_NBR;
-  const size_t fb = fa + H4 * K4 * DS_NBR;
-  const size_t base = (size_t)g * K4 * DS_NBR;
+  // output: column-major per frame, [frame][kx][ky]
+  const size_t fa = (size_t)(2 * pl) * K4 * P0;
+  const size_t fb = fa + (size_t)K4 * P0;
   for (int e = threadIdx.x; e < K4 * DS_NBR; e += T) {
     const int k = e / DS_NBR, r = e - k * DS_NBR;
+    const size_t o = (size_t)k * P0 + g * DS_NBR + r;
     float2 U = make_float2(0.0f, 0.0f), V = U;
     if (k <= P1 / 2) {
       const float2 zk = sm[r * LD + pidx(k)];
@@ -59,8 +61,8 @@ __global__ void __launch_bounds__(fft_threads(P1, DS_NBR))
       U = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
       V = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
     }
-    RW[fa + base + e] = U;
-    if (nb < N) RW[fb + base + e] = V;
+    RW[fa + o] = U;
+    if (nb < N) RW[fb + o] = V;
   }
 }
 
@@ -86,56 +88,60 @@ __device__ __forceinline__ void dose_weight(const zr_dose_params_t& p, int P0, i
   w = thres * filt;
 }
 
+// One column kx per CTA: for every frame, the column's forward FFT, times the
+// frame's filter, accumulated in registers (each thread owns P0/T rows).
+constexpr int DS_CT = 256;
+
 template <int P0>
-__global__ void __launch_bounds__(fft_threads(P0, DS_NBC))
+__global__ void __launch_bounds__(DS_CT, 2)
     k_dose_cols(const float2* __restrict__ RW, int f0, int nfr, int K4, int P1, zr_dose_params_t prm,
                 const float* __restrict__ thres_q, const float* __restrict__ dose_end, int first,
                 float2* __restrict__ ACC, float* __restrict__ FM, const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(P0, DS_NBC);
   constexpr int LD = ld_of(P0);
-  constexpr int H4 = P0 / DS_NBR;
+  constexpr int PER = P0 / DS_CT;
   extern __shared__ float2 sm[];
-  float2* acc = sm + DS_NBC * LD;                  // [DS_NBC][P0]
-  float* fm = (float*)(acc + DS_NBC * P0);          // [DS_NBC][P0]
-  const int k0 = blockIdx.x * DS_NBC;
-  for (int e = threadIdx.x; e < DS_NBC * P0; e += T) {
-    const int c = e / P0, y = e - c * P0;
-    acc[e] = first ? make_float2(0.0f, 0.0f) : ACC[(size_t)y * K4 + k0 + c];
-    fm[e] = (first || !prm.normalize) ? 0.0f : FM[(size_t)y * K4 + k0 + c];
+  const int kx = blockIdx.x;
+  float2 acc[PER];
+  float fm[PER];
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    const int y = threadIdx.x + j * DS_CT;
+    acc[j] = first ? make_float2(0.0f, 0.0f) : ACC[(size_t)kx * P0 + y];
+    fm[j] = (first || !prm.normalize) ? 0.0f : FM[(size_t)kx * P0 + y];
   }
   for (int nl = 0; nl < nfr; nl++) {
-    const float2* R = RW + (size_t)nl * H4 * K4 * DS_NBR;
+    const float4* col = reinterpret_cast<const float4*>(RW + ((size_t)nl * K4 + kx) * P0);
     __syncthreads();
-    for (int e = threadIdx.x; e < H4 * DS_NBC * DS_NBR; e += T) {
-      const int gg = e / (DS_NBC * DS_NBR), j = e - gg * (DS_NBC * DS_NBR);
-      const int c = j / DS_NBR, r = j - c * DS_NBR;
-      sm[c * LD + pidx(gg * DS_NBR + r)] = R[((size_t)gg * K4 + k0) * DS_NBR + j];
+    for (int e = threadIdx.x; e < P0 / 2; e += DS_CT) {
+      const float4 v = col[e];
+      sm[pidx(2 * e)] = make_float2(v.x, v.y);
+      sm[pidx(2 * e + 1)] = make_float2(v.z, v.w);
     }
     __syncthreads();
-    block_fft<P0, DS_NBC, T, -1>(sm, tw);
+    block_fft<P0, 1, DS_CT, -1>(sm, tw);
+    if (kx > P1 / 2) continue;
     const float de = dose_end[f0 + nl], tq = thres_q[f0 + nl];
-    for (int e = threadIdx.x; e < DS_NBC * P0; e += T) {
-      const int c = e / P0, y = e - c * P0;
-      const int kx = k0 + c;
-      if (kx > P1 / 2) continue;
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int y = threadIdx.x + j * DS_CT;
       float w;
       dose_weight(prm, P0, P1, y, kx, de, tq, w);
-      const float2 F = sm[c * LD + pidx(y)];
-      acc[e] = make_float2(acc[e].x + F.x * w, acc[e].y + F.y * w);
-      if (prm.normalize) fm[e] += w;
+      const float2 F = sm[pidx(y)];
+      acc[j] = make_float2(acc[j].x + F.x * w, acc[j].y + F.y * w);
+      if (prm.normalize) fm[j] += w;
     }
   }
-  __syncthreads();
-  for (int e = threadIdx.x; e < DS_NBC * P0; e += T) {
-    const int c = e / P0, y = e - c * P0;
-    ACC[(size_t)y * K4 + k0 + c] = acc[e];
-    if (prm.normalize) FM[(size_t)y * K4 + k0 + c] = fm[e];
+#pragma unroll
+  for (int j = 0; j < PER; j++) {
+    const int y = threadIdx.x + j * DS_CT;
+    ACC[(size_t)kx * P0 + y] = acc[j];
+    if (prm.normalize) FM[(size_t)kx * P0 + y] = fm[j];
   }
 }
 
 // Inverse column pass, keeping rows [0, H).
 template <int P0>
-__global__ void __launch_bounds__(fft_threads(P0, DS_NBR))
+__global__ void __launch_bounds__(fft_threads(P0, DS_NBR), fft_minblocks(P0))
     k_dose_icols(const float2* __restrict__ ACC, const float* __restrict__ FM, int normalize, int K4, int H,
                  float2* __restrict__ T2, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(P0, DS_NBR);
@@ -143,10 +149,10 @@ __global__ void __launch_bounds__(fft_threads(P0, DS_NBR))
   extern __shared__ float2 sm[];
   const int k0 = blockIdx.x * DS_NBR;
   for (int e = threadIdx.x; e < DS_NBR * P0; e += T) {
-    const int y = e / DS_NBR, c = e - y * DS_NBR;
-    float2 v = ACC[(size_t)y * K4 + k0 + c];
+    const int c = e / P0, y = e - c * P0;
+    float2 v = ACC[(size_t)(k0 + c) * P0 + y];
     if (normalize) {
-      const float s = 1.0f / (FM[(size_t)y * K4 + k0 + c] + 1.0f);
+      const float s = 1.0f / (FM[(size_t)(k0 + c) * P0 + y] + 1.0f);
       v = make_float2(v.x * s, v.y * s);
     }
     sm[c * LD + pidx(y)] = v;
@@ -161,7 +167,7 @@ __global__ void __launch_bounds__(fft_threads(P0, DS_NBR))
 
 // Real-output inverse row pass (two rows per complex FFT), |.|, crop, scale.
 template <int P1>
-__global__ void __launch_bounds__(fft_threads(P1, 2))
+__global__ void __launch_bounds__(fft_threads(P1, 2), fft_minblocks(P1))
     k_dose_irows(const float2* __restrict__ T2, int K4, int H, int W, float scale, float* __restrict__ out,
                  const float2* __restrict__ tw) {
   constexpr int T = fft_threads(P1, 2);
@@ -221,10 +227,9 @@ template <int P0>
 static int dose_cols(const float2* RW, int f0, int nfr, int K4, int P1, const zr_dose_params_t& prm,
                      const float* tq, const float* de, int first, float2* ACC, float* FM, const float2* tw,
                      cudaStream_t st) {
-  const size_t smem = (size_t)DS_NBC * ld_of(P0) * sizeof(float2) + (size_t)DS_NBC * P0 * (sizeof(float2) + sizeof(float));
+  const size_t smem = (size_t)ld_of(P0) * sizeof(float2);
   ZR_TRY(set_smem<P0>((const void*)k_dose_cols<P0>, smem));
-  k_dose_cols<P0><<<K4 / DS_NBC, fft_threads(P0, DS_NBC), smem, st>>>(RW, f0, nfr, K4, P1, prm, tq, de, first, ACC,
-                                                                       FM, tw);
+  k_dose_cols<P0><<<K4, DS_CT, smem, st>>>(RW, f0, nfr, K4, P1, prm, tq, de, first, ACC, FM, tw);
   return launched("k_dose_cols");
 }
 

@@ -3,7 +3,8 @@
 // A CTA transforms NB sequences of length L (a power of two, 2..8192) that sit
 // in shared memory.  Element i of sequence b lives at s[b*ld(L) + pidx(i)]:
 // one padding slot every 8 elements keeps the radix-8 scatter of the first
-// pass free of bank conflicts.  Each pass is a radix-8 (the last pass radix 2
+// pass free of bank conflicts, and the row pitch (ld_of) keeps tiles of 4
+// sequences x 4 elements conflict-free.  Each pass is a radix-8 (the last pass radix 2
 // or 4 when log2(L) is not a multiple of 3) Stockham step: every thread reads
 // its butterflies' inputs into registers, the CTA synchronises, and the
 // outputs are written back in place.  No ping-pong buffer is needed.
@@ -20,7 +21,12 @@ namespace zr {
 constexpr int TWN = 8192;  // twiddle table length
 
 __host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 3); }
-__host__ __device__ __forceinline__ constexpr int ld_of(int L) { return L + (L >> 3) + 1; }
+// Row pitch of one sequence: the padded length rounded so that pitch = 4
+// (mod 16) float2s; then 4 sequences x 4 consecutive elements (the tile the
+// row/column passes move per half-warp) fall on 32 distinct banks.
+__host__ __device__ __forceinline__ constexpr int ld_of(int L) {
+  return (((L + (L >> 3)) + 15) & ~15) + 4;
+}
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }

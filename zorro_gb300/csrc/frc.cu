@@ -19,15 +19,17 @@ namespace zr {
 constexpr int FRC_NB = 4;
 constexpr int FRC_TPG = 8;  // tiles accumulated per CTA of the column pass
 
-// Hann window of apodization('hann', box): radius box/2, circular.
+// Hann window of apodization('hann', box): radius box/2, circular.  The
+// squared radius is exact in float for power-of-two boxes.
 __device__ __forceinline__ float hann_at(int y, int x, int B) {
-  const double yy = (double)(y - B / 2) / (B / 2.0), xx = (double)(x - B / 2) / (B / 2.0);
-  const double rr = xx * xx + yy * yy;
-  return rr <= 1.0 ? (float)(0.5 * (1.0 + cos(M_PI * sqrt(rr)))) : 0.0f;
+  const float inv = 2.0f / (float)B;
+  const float yy = (float)(y - B / 2) * inv, xx = (float)(x - B / 2) * inv;
+  const float rr = xx * xx + yy * yy;
+  return rr <= 1.0f ? 0.5f * (1.0f + cospif(sqrtf(rr))) : 0.0f;
 }
 
 template <int B>
-__global__ void __launch_bounds__(fft_threads(B, FRC_NB))
+__global__ void __launch_bounds__(fft_threads(B, FRC_NB), fft_minblocks(B))
     k_frc_rows(const float* __restrict__ even, const float* __restrict__ odd, int W, const int* __restrict__ offs,
                int K4, float2* __restrict__ RE, float2* __restrict__ RO, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(B, FRC_NB);
@@ -60,7 +62,7 @@ __global__ void __launch_bounds__(fft_threads(B, FRC_NB))
 }
 
 template <int B>
-__global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB))
+__global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB), fft_minblocks(B))
     k_frc_cols(const float2* __restrict__ RE, const float2* __restrict__ RO, int n_tiles, int K4,
                double* __restrict__ half, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(B, 2 * FRC_NB);

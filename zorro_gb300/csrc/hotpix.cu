@@ -31,6 +31,30 @@ __global__ void k_gain_sum(FrameSrc f, float* __restrict__ sum, double* __restri
   }
 }
 
+// Same sum, four pixels per thread with vector loads (H*W % 4 == 0).
+__global__ void k_gain_sum4(FrameSrc f, float* __restrict__ sum, double* __restrict__ total) {
+  const long long n4 = (long long)f.H * f.W / 4;
+  double part = 0.0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int n = 0; n < f.N; n++) {
+      const float4 v = load4_corrected(f, n, 4 * q);
+      s = make_float4(__fadd_rn(s.x, v.x), __fadd_rn(s.y, v.y), __fadd_rn(s.z, v.z), __fadd_rn(s.w, v.w));
+    }
+    reinterpret_cast<float4*>(sum)[q] = s;
+    part += (double)s.x + (double)s.y + (double)s.z + (double)s.w;
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0 && total) atomicAdd(total, v);
+  }
+}
+
 __global__ void k_histogram(const float* __restrict__ v, long long n, double e0, int nbins, unsigned int* __restrict__ counts) {
   extern __shared__ unsigned int hist[];
   for (int i = threadIdx.x; i < nbins; i += blockDim.x) hist[i] = 0;
@@ -156,6 +180,12 @@ extern "C" int zr_gain_sum(const zr_frames_t* frames, float* unaligned_sum, doub
   f.hb = nullptr;
   if (f.N <= 0 || f.H <= 0 || f.W <= 0) return set_error(ZR_EINVAL, "zr_gain_sum: empty movie");
   const long long npix = (long long)f.H * f.W;
+  if (npix % 4 == 0 && f.fstride % 4 == 0 && ((uintptr_t)unaligned_sum & 15) == 0) {
+    int blocks = (int)((npix / 4 + 255) / 256);
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_gain_sum4<<<blocks, 256, 0, (cudaStream_t)stream>>>(f, unaligned_sum, total);
+    return launched("k_gain_sum4");
+  }
   int blocks = (int)((npix + 255) / 256);
   if (blocks > 152 * 16) blocks = 152 * 16;
   k_gain_sum<<<blocks, 256, 0, (cudaStream_t)stream>>>(f, unaligned_sum, total);

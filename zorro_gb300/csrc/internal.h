@@ -20,10 +20,19 @@ inline int ilog2(long long v) {
   return l;
 }
 
-// Threads for a batched shared-memory FFT of NB sequences of length L.
+// Threads for a batched shared-memory FFT of NB sequences of length L:
+// ZR_FFT_EPT elements per thread and pass (radix-8 butterflies of 8).
+#ifndef ZR_FFT_EPT
+#define ZR_FFT_EPT 32
+#endif
+#ifndef ZR_FFT_MINB
+#define ZR_FFT_MINB 1
+#endif
 constexpr int fft_threads(int L, int NB) {
-  return (NB * L / 32 < 64) ? 64 : ((NB * L / 32 > 512) ? 512 : NB * L / 32);
+  return (NB * L / ZR_FFT_EPT < 64) ? 64 : ((NB * L / ZR_FFT_EPT > 512) ? 512 : NB * L / ZR_FFT_EPT);
 }
+// Resident CTAs per SM to ask the register allocator for (short transforms).
+constexpr int fft_minblocks(int L) { return L <= 2048 ? ZR_FFT_MINB : 1; }
 
 }  // namespace zr
 

@@ -205,6 +205,101 @@ __device__ void filter_pass(const float* C, float* V, const int* rtab, int w, in
   }
 }
 
+// The same visit for w % 4 == 0 with the work vectorised: each thread
+// filters 4 consecutive columns; the vertical taps are float4 loads, the
+// horizontal taps slide a 4-wide register window one column at a time.
+template <int MODE>
+__device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx,
+                             const float* wy, const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st,
+                             float& amax, int& aidx) {
+  const int tx = threadIdx.x & (PK_TX - 1), ty = threadIdx.x / PK_TX;
+  const int w4 = w >> 2;
+  float s1 = 0.0f, s2 = 0.0f, mx = -INFINITY;
+  float bv = -INFINITY;
+  int bi = 0x7fffffff;
+  int cnt = 0;
+  for (int y0 = 0; y0 < w; y0 += PK_RB) {
+    const int y = y0 + ty;
+    if (y < w && tx < w4) {
+      const int x0 = tx << 2;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      const bool interior = (y >= ry && y + ry < w);
+      const float* p = C + (y - ry) * w + x0;
+      const int* rt = rtab + PK_MAXR + y - ry;
+      for (int k = 0; k <= 2 * ry; k++) {
+        const float4 v = *reinterpret_cast<const float4*>(interior ? p + k * w : C + rt[k] * w + x0);
+        const float wk = wy[k];
+        acc.x = fmaf(wk, v.x, acc.x); acc.y = fmaf(wk, v.y, acc.y);
+        acc.z = fmaf(wk, v.z, acc.z); acc.w = fmaf(wk, v.w, acc.w);
+      }
+      *reinterpret_cast<float4*>(V + ty * w + x0) = acc;
+    }
+    __syncthreads();
+    if (y < w && tx < w4) {
+      const float* vr = V + ty * w;
+      const int x0 = tx << 2;
+      const bool interior = (x0 >= rx && x0 + 3 + rx < w);
+      const int* rt = rtab + PK_MAXR + x0 - rx;
+      const float* q = vr + x0 - rx;
+      float a0 = interior ? q[0] : vr[rt[0]];
+      float a1 = interior ? q[1] : vr[rt[1]];
+      float a2 = interior ? q[2] : vr[rt[2]];
+      float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+      for (int k = 0; k <= 2 * rx; k++) {
+        const float a3 = interior ? q[k + 3] : vr[rt[k + 3]];
+        const float wk = wx[k];
+        f0 = fmaf(wk, a0, f0); f1 = fmaf(wk, a1, f1); f2 = fmaf(wk, a2, f2); f3 = fmaf(wk, a3, f3);
+        a0 = a1; a1 = a2; a2 = a3;
+      }
+      const float fv[4] = {f0, f1, f2, f3};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const float f = fv[j];
+        const int x = x0 + j;
+        bool in = true;
+        if (MODE == 1) {
+          const int dy = y - mS, dx = x - mS;
+          in = !use_mask || (dy * dy + dx * dx < mS * mS);
+          const float mv = in ? f : 0.0f;
+          const int idx = y * w + x;
+          if (mv > bv || (mv == bv && idx < bi)) { bv = mv; bi = idx; }
+        }
+        if (in) {
+          const float d = f - c;
+          s1 += d;
+          s2 = fmaf(d, d, s2);
+          mx = fmaxf(mx, f);
+          cnt++;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  double3 r = block_sum3(sh, (double)s1, (double)s2, (double)cnt);
+  st.s1 = r.x;
+  st.s2 = r.y;
+  st.n = (int)r.z;
+  float m = mx;
+  int dummy = 0;
+  block_argmax(sh, m, dummy);
+  st.mx = m;
+  if (MODE == 1) {
+    block_argmax(sh, bv, bi);
+    amax = bv;
+    aidx = bi;
+  }
+}
+
+template <int MODE>
+__device__ void filter_any(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx, const float* wy,
+                           const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st, float& amax,
+                           int& aidx) {
+  if ((w & 3) == 0 && w <= 4 * PK_TX)
+    filter_pass4<MODE>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
+  else
+    filter_pass<MODE>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
+}
+
 __device__ double objective(const float* C, float* V, const int* rtab, int w, int mS, double sigma, float c,
                             PkShared& sh) {
   const int r = gauss_weights(sigma, sh.wy);
@@ -212,7 +307,7 @@ __device__ double objective(const float* C, float* V, const int* rtab, int w, in
   FiltStats st;
   float am;
   int ai;
-  filter_pass<0>(C, V, rtab, w, mS, r, r, sh.wy, sh.wy, c, sh, false, st, am, ai);
+  filter_any<0>(C, V, rtab, w, mS, r, r, sh.wy, sh.wy, c, sh, false, st, am, ai);
   const double n = (double)st.n;
   const double m1 = st.s1 / n;
   const double var = st.s2 / n - m1 * m1;
@@ -354,7 +449,7 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
   FiltStats st;
   float amax = 0.0f;
   int aidx = 0;
-  filter_pass<1>(C, V, rtab, w, mS, ry, rx, sh.wy, sh.wx, c, sh, p.use_mask != 0, st, amax, aidx);
+  filter_any<1>(C, V, rtab, w, mS, ry, rx, sh.wy, sh.wx, c, sh, p.use_mask != 0, st, amax, aidx);
   const int cy = aidx / w, cx = aidx - (aidx / w) * w;
   double peaksig = nan("");
   {

@@ -3,7 +3,7 @@
 // lazyFouRingCorr (zorro.py:2237-2238), in one pass over the raw frames.
 //
 // Frame n is rolled by (roll_y, roll_x) (np.roll: out[i] = in[i - shift],
-// circular), then convolved with the separable 3x3 kernel ky (x) kx
+// circular; the offsets are given reduced to [0, H) and [0, W)), then convolved with the separable 3x3 kernel ky (x) kx
 // (scipy.ndimage.convolve: out[i] = sum_k w[k] in[i - k + 1], 'reflect'
 // borders of the rolled frame).  Sums run over frames in order in float32,
 // as np.sum(images, axis=0) does for a float32 stack.
@@ -35,9 +35,10 @@ __global__ void __launch_bounds__(SS_THR)
       const int Y = refl1(y0 - 1 + i, H), X = refl1(x0 - 1 + j, W);
       float v = 0.0f;
       if (y0 - 1 + i < H + 1 && x0 - 1 + j < W + 1) {
-        int sy = (Y - t.roll_y) % H;
+        // roll offsets arrive reduced to [0, H) and [0, W)
+        int sy = Y - t.roll_y;
         if (sy < 0) sy += H;
-        int sx = (X - t.roll_x) % W;
+        int sx = X - t.roll_x;
         if (sx < 0) sx += W;
         v = load_corrected(f, n, sy, sx);
       }

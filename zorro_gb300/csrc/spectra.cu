@@ -19,7 +19,7 @@ namespace zr {
 constexpr int NBR = 4;  // rows / columns per CTA
 
 template <int P1>
-__global__ void __launch_bounds__(fft_threads(P1, NBR))
+__global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
     k_fwd_rows(FrameSrc f, const float* __restrict__ mask, const double* __restrict__ mean_sub,
                double inv_area, int frame0, int mode, int rows, int cols, int C1, int K4, int H4,
                float2* __restrict__ RU, float2* __restrict__ RV, const float2* __restrict__ tw) {
@@ -33,20 +33,69 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR))
   const int n = frame0 + nl;
   float mu = 0.0f;
   if (mode == 0 && mean_sub) mu = (float)(mean_sub[n] * inv_area);
-  for (int e = threadIdx.x; e < NBR * P1; e += T) {
-    const int r = e / P1, x = e - (e / P1) * P1;
-    const int y = g * NBR + r;
-    float2 z = make_float2(0.0f, 0.0f);
-    if (y < rows && x < cols) {
-      const float m = mask ? __ldg(mask + (size_t)y * P1 + x) : 1.0f;
-      if (mode == 0) {
-        const float u = m * (load_corrected(f, n, y, x) - mu);
-        z = make_float2(u, u * u);
+  if (mode == 0 && !mask && (f.fstride & 3) == 0) {
+    // 4 pixels per thread and step: aligned vector loads of the raw frame and
+    // every map; the unaligned head (< 4 pixels) and tail go pixel by pixel
+    for (int e = threadIdx.x; e < NBR * (P1 / 4); e += T) {
+      const int r = e / (P1 / 4), q = e - r * (P1 / 4);
+      const int y = g * NBR + r;
+      float2* srow = sm + r * LD;
+      if (y >= rows) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) srow[pidx(4 * q + j)] = make_float2(0.0f, 0.0f);
+        continue;
+      }
+      const long long p0 = (long long)y * f.W;
+      const int off = (int)((4 - (p0 & 3)) & 3);  // first x with (p0 + x) % 4 == 0
+      const int x = off + 4 * q;
+      if (x + 3 < cols) {
+        const float4 v = load4_corrected(f, n, p0 + x);
+        const float u0 = v.x - mu, u1 = v.y - mu, u2 = v.z - mu, u3 = v.w - mu;
+        srow[pidx(x)] = make_float2(u0, u0 * u0);
+        srow[pidx(x + 1)] = make_float2(u1, u1 * u1);
+        srow[pidx(x + 2)] = make_float2(u2, u2 * u2);
+        srow[pidx(x + 3)] = make_float2(u3, u3 * u3);
       } else {
-        z.x = m;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int xx = x + j;
+          if (xx < P1) {
+            float2 z = make_float2(0.0f, 0.0f);
+            if (xx < cols) {
+              const float u = load_corrected(f, n, y, xx) - mu;
+              z = make_float2(u, u * u);
+            }
+            srow[pidx(xx)] = z;
+          }
+        }
+      }
+      if (q == 0) {
+        for (int xx = 0; xx < off; xx++) {
+          float2 z = make_float2(0.0f, 0.0f);
+          if (xx < cols) {
+            const float u = load_corrected(f, n, y, xx) - mu;
+            z = make_float2(u, u * u);
+          }
+          srow[pidx(xx)] = z;
+        }
       }
     }
-    sm[r * LD + pidx(x)] = z;
+  } else {
+    for (int e = threadIdx.x; e < NBR * P1; e += T) {
+      const int r = e / P1, x = e - (e / P1) * P1;
+      const int y = g * NBR + r;
+      float2 z = make_float2(0.0f, 0.0f);
+      if (y < rows && x < cols) {
+        const float m = mask ? __ldg(mask + (size_t)y * P1 + x) : 1.0f;
+        if (mode == 0) {
+          const float u = m * (load_corrected(f, n, y, x) - mu);
+          z = make_float2(u, u * u);
+        } else {
+          z.x = m;
+        }
+      }
+      sm[r * LD + pidx(x)] = z;
+    }
   }
   __syncthreads();
   block_fft<P1, NBR, T, -1>(sm, tw);
@@ -67,7 +116,7 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR))
 }
 
 template <int P0>
-__global__ void __launch_bounds__(fft_threads(P0, NBR))
+__global__ void __launch_bounds__(fft_threads(P0, NBR), fft_minblocks(P0))
     k_fwd_cols(const float2* __restrict__ RU, const float2* __restrict__ RV, int rows, int C0, int K4, int H4,
                long long spec_elems, float2* __restrict__ G, float2* __restrict__ S,
                const float2* __restrict__ tw) {
@@ -93,10 +142,11 @@ __global__ void __launch_bounds__(fft_threads(P0, NBR))
   __syncthreads();
   block_fft<P0, NBR, T, -1>(sm, tw);
   const int hc = C0 / 2;
+  const int RP = C0 + 4;
   for (int e = threadIdx.x; e < (C0 + 1) * NBR; e += T) {
-    const int r = e / NBR, c = e - r * NBR;
+    const int c = e / (C0 + 1), r = e - c * (C0 + 1);
     const int ky = r < hc ? r : (r < C0 ? P0 - C0 + r : hc);
-    out[(size_t)r * K4 + k0 + c] = sm[c * LD + pidx(ky)];
+    out[(size_t)(k0 + c) * RP + r] = sm[c * LD + pidx(ky)];
   }
 }
 
@@ -166,7 +216,7 @@ using namespace zr;
 
 extern "C" int zr_spectrum_pitch(int C1) { return ((C1 / 2 + 1) + 3) & ~3; }
 
-extern "C" long long zr_spectrum_elems(int C0, int C1) { return (long long)(C0 + 1) * zr_spectrum_pitch(C1); }
+extern "C" long long zr_spectrum_elems(int C0, int C1) { return (long long)(C0 + 4) * zr_spectrum_pitch(C1); }
 
 extern "C" size_t zr_spectra_work_bytes(int height, int n_frames, int C1) {
   const size_t H4 = (size_t)(height + 3) / 4;

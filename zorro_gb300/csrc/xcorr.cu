@@ -55,7 +55,7 @@ __device__ __forceinline__ void job_operands(const XcJobs& J, int job, const flo
 }
 
 template <int C0>
-__global__ void __launch_bounds__(fft_threads(C0, XC_NBC))
+__global__ void __launch_bounds__(fft_threads(C0, XC_NBC), fft_minblocks(C0))
     k_xc_cols(XcJobs J, int C1, int K4, int mS, float2* __restrict__ Tw, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(C0, XC_NBC);
   constexpr int LD = ld_of(C0);
@@ -67,23 +67,30 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC))
   const float2 *A, *B;
   job_operands(J, J.job0 + jl, A, B);
   const int half = C1 / 2, hc = C0 / 2;
-  for (int e = threadIdx.x; e < C0 * XC_NBC; e += T) {
-    const int r = e / XC_NBC, c = e - r * XC_NBC;
+  const int RP = C0 + 4;  // column pitch of the spectra
+  // two rows per element: 16-byte loads along each (contiguous) column
+  for (int e = threadIdx.x; e < (C0 / 2) * XC_NBC; e += T) {
+    const int c = e / (C0 / 2), r = 2 * (e - c * (C0 / 2));
     const int k = k0 + c;
-    float2 h = make_float2(0.0f, 0.0f);
-    if (k == 0) {
-      h = cmulc(A[(size_t)r * K4], B[(size_t)r * K4]);
-    } else if (k < half) {
-      h = cmulc(A[(size_t)r * K4 + k], B[(size_t)r * K4 + k]);
-      if (r == hc) {
-        const float2 h2 = cmulc(A[(size_t)C0 * K4 + k], B[(size_t)C0 * K4 + k]);
-        h = make_float2(0.5f * (h.x + h2.x), 0.5f * (h.y + h2.y));
+    float2 h0 = make_float2(0.0f, 0.0f), h1 = h0;
+    if (k < half) {
+      const float4 a = *reinterpret_cast<const float4*>(A + (size_t)k * RP + r);
+      const float4 b = *reinterpret_cast<const float4*>(B + (size_t)k * RP + r);
+      h0 = cmulc(make_float2(a.x, a.y), make_float2(b.x, b.y));
+      h1 = cmulc(make_float2(a.z, a.w), make_float2(b.z, b.w));
+      if (k > 0 && r == hc) {
+        const float2 h2 = cmulc(A[(size_t)k * RP + C0], B[(size_t)k * RP + C0]);
+        h0 = make_float2(0.5f * (h0.x + h2.x), 0.5f * (h0.y + h2.y));
       }
     } else if (k == half) {
-      const int m = (r == 0) ? 0 : (r == hc ? C0 : C0 - r);
-      h = cmulc(B[(size_t)m * K4 + k], A[(size_t)m * K4 + k]);  // conj(A) * B
+      const float2* Ak = A + (size_t)k * RP;
+      const float2* Bk = B + (size_t)k * RP;
+      const int m0 = (r == 0) ? 0 : (r == hc ? C0 : C0 - r), m1 = C0 - r - 1;
+      h0 = cmulc(Bk[m0], Ak[m0]);  // conj(A) * B at the mirrored row
+      h1 = cmulc(Bk[m1], Ak[m1]);
     }
-    sm[c * LD + pidx(r)] = h;
+    sm[c * LD + pidx(r)] = h0;
+    sm[c * LD + pidx(r + 1)] = h1;
   }
   __syncthreads();
   block_fft<C0, XC_NBC, T, 1>(sm, tw);
@@ -97,7 +104,7 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC))
 }
 
 template <int C1>
-__global__ void __launch_bounds__(fft_threads(C1, XC_NBR))
+__global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
     k_xc_rows(XcJobs J, int C0, int K4, int mS, float scale, const float2* __restrict__ Tw,
               const float* __restrict__ terms, float* __restrict__ out, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(C1, XC_NBR);

@@ -359,7 +359,7 @@ class Engine:
             params = hm.shift_params(translations)
         sh = (Shift * N)()
         for n, (ry, rx, ap, ky, kx) in enumerate(params):
-            sh[n].roll_y, sh[n].roll_x, sh[n].apply = ry, rx, ap
+            sh[n].roll_y, sh[n].roll_x, sh[n].apply = ry % H, rx % W, ap
             for i in range(3):
                 sh[n].ky[i] = float(ky[i])
                 sh[n].kx[i] = float(kx[i])
