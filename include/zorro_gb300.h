@@ -202,6 +202,17 @@ int zr_tiled_frc(const float* even, const float* odd, int height, int width, int
                  const int* offsets, int n_tiles, float* frc2d, double* frc, int nrings,
                  void* work, size_t work_bytes, void* stream);
 
+/* ---- drift solve: shiftsSolver, zorro.py:1260-1567 (host only) ---- */
+
+/* Exact weighted L1 regression on the host: x = argmin sum_i w_i |(A x)_i - b_i|,
+ * the objective of shiftsSolver (zorro_util.py:849-851), which the reference
+ * minimises with scipy.optimize.basinhopping (zorro.py:1415,1422).  A, b, w, x
+ * are HOST arrays (A row-major [m][n]).  *status: 0 optimum found inside
+ * [lo, hi]; 4 optimum found but outside the box (the caller solves the bounded
+ * problem instead). */
+int zr_l1_solve(const double* A, const double* b, const double* w, int m, int n, double lo, double hi,
+                double* x, int* status);
+
 /* ---- dose filter: doseFilter, zorro.py:2349-2494 ---- */
 
 size_t zr_dose_work_bytes(int P0, int P1, int n_frames);

@@ -19,6 +19,7 @@ EXPORTS = (
     "zr_hotpix_maps", "zr_frame_sums", "zr_spectrum_pitch", "zr_spectrum_elems", "zr_spectra_work_bytes",
     "zr_spectra", "zr_xcorr_work_bytes", "zr_xcorr_terms", "zr_xcorr_pairs", "zr_locate_peaks",
     "zr_shift_sum", "zr_frc_work_bytes", "zr_tiled_frc", "zr_dose_work_bytes", "zr_dose_filter",
+    "zr_l1_solve",
 )
 
 
@@ -90,6 +91,7 @@ _SIGS = {
     "zr_tiled_frc": (C.c_int, [_P, _P, C.c_int, C.c_int, C.c_int, _P, C.c_int, _P, _P, C.c_int, _P, C.c_size_t,
                                _P]),
     "zr_dose_work_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int]),
+    "zr_l1_solve": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, C.c_double, C.c_double, _P, C.POINTER(C.c_int)]),
     "zr_dose_filter": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.POINTER(DoseParams), _P, _P, C.c_int, C.c_int,
                                  _P, _P, C.c_size_t, _P]),
 }

@@ -65,17 +65,22 @@ def equation_matrix(tri):
 
 def l1_solve(A, b, w, lo, hi):
     """argmin_x sum(w * |A x - b|) with lo <= x <= hi (the objective of
-    zorro_util.py:849-851), exactly.  The dual linear programme
-    (max b.y s.t. A^T y = 0, |y| <= w) has only n equality rows; its
-    equality multipliers are the primal optimum.  If that point leaves the
-    box, the bounded primal LP is solved instead."""
+    zorro_util.py:849-851), exactly.  The native simplex of libzorrogb
+    (zr_l1_solve) solves the dual linear programme (max b.y s.t. A^T y = 0,
+    |y| <= w), whose equality multipliers are the primal optimum.  If that
+    point leaves the box, the bounded primal LP is solved instead."""
+    import ctypes as C
+    from . import _lib
     m, n = A.shape
-    w = np.asarray(w, dtype=np.float64)
-    res = scipy.optimize.linprog(-b, A_eq=A.T, b_eq=np.zeros(n), bounds=list(zip(-w, w)), method="highs")
-    if res.success:
-        x = -res.eqlin.marginals
-        if np.all(x >= lo) and np.all(x <= hi):
-            return x
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    Ac = np.ascontiguousarray(A, dtype=np.float64)
+    bc = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    st = C.c_int(-1)
+    rc = _lib.load().zr_l1_solve(Ac.ctypes.data, bc.ctypes.data, w.ctypes.data, m, n, float(lo), float(hi),
+                                 x.ctypes.data, C.byref(st))
+    if rc == 0 and st.value == 0:
+        return x
     cost = np.concatenate([np.zeros(n), w])
     eye = np.eye(m)
     A_ub = np.block([[A, -eye], [-A, -eye]])
