@@ -21,7 +21,9 @@ Two exact reformulations of the reference's arithmetic are used:
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
+import threading
 import time
 
 import numpy as np
@@ -63,8 +65,11 @@ class Engine:
         self.lib = _lib.load()
         with torch.cuda.device(self.dev):
             _lib.call("zr_init", device)
-        self.bufs = {}
+        self._slots = {}
+        self._slots_lock = threading.Lock()
+        self._tls = threading.local()
         self.profile = None  # dict stage -> list of (start, end) CUDA events when enabled
+        self._profile_lock = threading.Lock()
 
     def call(self, stage, name, *args):
         """One C-ABI call; bracketed by CUDA events on the current stream when
@@ -77,7 +82,8 @@ class Engine:
         e0.record()
         rc = _lib.call(name, *args)
         e1.record()
-        self.profile.setdefault(stage, []).append((e0, e1))
+        with self._profile_lock:
+            self.profile.setdefault(stage, []).append((e0, e1))
         return rc
 
     def stage_ms(self):
@@ -85,12 +91,38 @@ class Engine:
         self.torch.cuda.synchronize(self.dev)
         return {k: sum(a.elapsed_time(b) for a, b in v) for k, v in (self.profile or {}).items()}
 
-    # ------------------------------------------------------------------ buffers
+    # ------------------------------------------------------------------ slots and buffers
+    def _slot(self, slot):
+        """Per-slot state: a buffer pool and (except slot 0, which uses the
+        caller's current stream) a stream of its own.  Movies registered in
+        different slots can run concurrently from different threads."""
+        with self._slots_lock:
+            st = self._slots.get(slot)
+            if st is None:
+                stream = None if slot == 0 else self.torch.cuda.Stream(device=self.dev)
+                st = self._slots[slot] = {"bufs": {}, "stream": stream}
+            return st
+
+    @property
+    def bufs(self):
+        st = getattr(self._tls, "slot", None)
+        return st["bufs"] if st is not None else self._slot(0)["bufs"]
+
+    def slot_bytes(self, slot=None):
+        """Device bytes held by one slot's buffers (all slots when None)."""
+        with self._slots_lock:
+            slots = list(self._slots.values()) if slot is None else [self._slots.get(slot, {"bufs": {}})]
+        return sum(t.numel() for st in slots for t in st["bufs"].values())
+
     def buf(self, name, nbytes):
-        t = self.bufs.get(name)
+        bufs = self.bufs
+        t = bufs.get(name)
         if t is None or t.numel() < nbytes:
+            if t is not None:
+                del bufs[name]
+                t = None
             t = self.torch.empty(max(int(nbytes), 1), dtype=self.torch.uint8, device=self.dev)
-            self.bufs[name] = t
+            bufs[name] = t
         return t
 
     def ptr(self, name, nbytes):
@@ -133,10 +165,20 @@ class Engine:
         return t, gain, _RAW_TYPES[dt]
 
     # ------------------------------------------------------------------ pipeline
-    def align(self, reg):
+    def align(self, reg, slot=0):
+        """Register one movie (all outputs set on ``reg``).  ``slot`` selects
+        the buffer pool and stream; one thread per slot at a time."""
         torch = self.torch
-        with torch.cuda.device(self.dev):
-            res = self._align(reg)
+        st = self._slot(slot)
+        self._tls.slot = st
+        try:
+            sctx = torch.cuda.stream(st["stream"]) if st["stream"] is not None else contextlib.nullcontext()
+            with torch.cuda.device(self.dev), sctx:
+                res = self._align(reg)
+                if st["stream"] is not None:
+                    st["stream"].synchronize()
+        finally:
+            self._tls.slot = None
         for k, v in res.items():
             setattr(reg, k, v)
 
