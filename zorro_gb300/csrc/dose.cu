@@ -100,7 +100,25 @@ __global__ void __launch_bounds__(DS_CT, 2)
   constexpr int LD = ld_of(P0);
   constexpr int PER = P0 / DS_CT;
   extern __shared__ float2 sm[];
+  // per-element constants of this column: 1/critDose(q) and log2(q)
+  float* inv_crit = reinterpret_cast<float*>(sm + LD);
+  float* lq = inv_crit + P0;
   const int kx = blockIdx.x;
+  const bool live = kx <= P1 / 2;
+  for (int y = threadIdx.x; y < P0 && live; y += DS_CT) {
+    const int fy = y < P0 / 2 ? y : y - P0;
+    const float q = sqrtf((float)kx * (float)kx * (prm.inv_ps_x * prm.inv_ps_x) +
+                          (float)fy * (float)fy * (prm.inv_ps_y * prm.inv_ps_y));
+    float crit;
+    if (y == P0 / 2 && kx == P1 / 2) {
+      const float c = crit_dose(prm, fy, P1 / 2 - 1);
+      crit = c * c;  // zorro.py:2422
+    } else {
+      crit = prm.voltage_scaling * (prm.crit_a * powf(q, prm.crit_b) + prm.crit_c);
+    }
+    inv_crit[y] = 1.0f / crit;
+    lq[y] = log2f(q);
+  }
   float2 acc[PER];
   float fm[PER];
 #pragma unroll
@@ -109,6 +127,7 @@ __global__ void __launch_bounds__(DS_CT, 2)
     acc[j] = first ? make_float2(0.0f, 0.0f) : ACC[(size_t)kx * P0 + y];
     fm[j] = (first || !prm.normalize) ? 0.0f : FM[(size_t)kx * P0 + y];
   }
+  const float LOG2E = 1.4426950408889634f;
   for (int nl = 0; nl < nfr; nl++) {
     const float4* col = reinterpret_cast<const float4*>(RW + ((size_t)nl * K4 + kx) * P0);
     __syncthreads();
@@ -119,13 +138,16 @@ __global__ void __launch_bounds__(DS_CT, 2)
     }
     __syncthreads();
     block_fft<P0, 1, DS_CT, -1>(sm, tw);
-    if (kx > P1 / 2) continue;
-    const float de = dose_end[f0 + nl], tq = thres_q[f0 + nl];
+    if (!live) continue;
+    // filt = exp(-0.5 D / crit), thres = exp(-(q / thresQ)^order)
+    const float cd = (-0.5f * dose_end[f0 + nl]) * LOG2E;
+    const float ltq = log2f(thres_q[f0 + nl]);
 #pragma unroll
     for (int j = 0; j < PER; j++) {
       const int y = threadIdx.x + j * DS_CT;
-      float w;
-      dose_weight(prm, P0, P1, y, kx, de, tq, w);
+      const float filt = exp2f(cd * inv_crit[y]);
+      const float thres = exp2f(-LOG2E * exp2f(prm.cutoff_order * (lq[y] - ltq)));
+      const float w = thres * filt;
       const float2 F = sm[pidx(y)];
       acc[j] = make_float2(acc[j].x + F.x * w, acc[j].y + F.y * w);
       if (prm.normalize) fm[j] += w;
@@ -227,7 +249,7 @@ template <int P0>
 static int dose_cols(const float2* RW, int f0, int nfr, int K4, int P1, const zr_dose_params_t& prm,
                      const float* tq, const float* de, int first, float2* ACC, float* FM, const float2* tw,
                      cudaStream_t st) {
-  const size_t smem = (size_t)ld_of(P0) * sizeof(float2);
+  const size_t smem = (size_t)ld_of(P0) * sizeof(float2) + (size_t)2 * P0 * sizeof(float);
   ZR_TRY(set_smem<P0>((const void*)k_dose_cols<P0>, smem));
   k_dose_cols<P0><<<K4, DS_CT, smem, st>>>(RW, f0, nfr, K4, P1, prm, tq, de, first, ACC, FM, tw);
   return launched("k_dose_cols");

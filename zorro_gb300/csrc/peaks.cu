@@ -212,15 +212,17 @@ template <int MODE>
 __device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx,
                              const float* wy, const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st,
                              float& amax, int& aidx) {
-  const int tx = threadIdx.x & (PK_TX - 1), ty = threadIdx.x / PK_TX;
+  // w/4 column lanes (each 4 columns wide) x RB rows of a block
   const int w4 = w >> 2;
+  const int RB = PK_T / w4;
+  const int tx = threadIdx.x % w4, ty = threadIdx.x / w4;
   float s1 = 0.0f, s2 = 0.0f, mx = -INFINITY;
   float bv = -INFINITY;
   int bi = 0x7fffffff;
   int cnt = 0;
-  for (int y0 = 0; y0 < w; y0 += PK_RB) {
+  for (int y0 = 0; y0 < w; y0 += RB) {
     const int y = y0 + ty;
-    if (y < w && tx < w4) {
+    if (y < w && ty < RB) {
       const int x0 = tx << 2;
       float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
       const bool interior = (y >= ry && y + ry < w);
@@ -235,7 +237,7 @@ __device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, i
       *reinterpret_cast<float4*>(V + ty * w + x0) = acc;
     }
     __syncthreads();
-    if (y < w && tx < w4) {
+    if (y < w && ty < RB) {
       const float* vr = V + ty * w;
       const int x0 = tx << 2;
       const bool interior = (x0 >= rx && x0 + 3 + rx < w);
@@ -294,7 +296,7 @@ template <int MODE>
 __device__ void filter_any(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx, const float* wy,
                            const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st, float& amax,
                            int& aidx) {
-  if ((w & 3) == 0 && w <= 4 * PK_TX)
+  if ((w & 3) == 0 && w >= 16 && w <= 4 * PK_TX)
     filter_pass4<MODE>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
   else
     filter_pass<MODE>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
@@ -572,9 +574,12 @@ extern "C" int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr
     return set_error(ZR_ESIZE, "zr_locate_peaks: opti sigma bound too large");
   const float2* tw = twiddles();
   if (!tw) return ZR_ECUDA;
-  size_t smem = (size_t)w * w * sizeof(float) + (size_t)PK_RB * w * sizeof(float);
+  // window + one block of filtered rows (at most PK_T*4 floats for the
+  // vectorised layout, PK_RB rows otherwise)
+  const size_t vbuf = (size_t)((4 * PK_T > PK_RB * w) ? 4 * PK_T : PK_RB * w) * sizeof(float);
+  size_t smem = (size_t)w * w * sizeof(float) + vbuf;
   const size_t sub = (size_t)16 * 16 * params->sub_pix_reg * sizeof(float2);
-  if (params->sub_pix_reg > 1 && (size_t)w * w * sizeof(float) < sub) smem = sub + (size_t)PK_RB * w * sizeof(float);
+  if (params->sub_pix_reg > 1 && (size_t)w * w * sizeof(float) < sub) smem = sub + vbuf;
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_peaks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_peaks attr"));
   k_peaks<<<M, PK_T, smem, (cudaStream_t)stream>>>(cwin, max_shift, *params, results, tw);

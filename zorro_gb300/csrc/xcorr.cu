@@ -68,29 +68,50 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC), fft_minblocks(C0))
   job_operands(J, J.job0 + jl, A, B);
   const int half = C1 / 2, hc = C0 / 2;
   const int RP = C0 + 4;  // column pitch of the spectra
-  // two rows per element: 16-byte loads along each (contiguous) column
-  for (int e = threadIdx.x; e < (C0 / 2) * XC_NBC; e += T) {
-    const int c = e / (C0 / 2), r = 2 * (e - c * (C0 / 2));
-    const int k = k0 + c;
-    float2 h0 = make_float2(0.0f, 0.0f), h1 = h0;
-    if (k < half) {
-      const float4 a = *reinterpret_cast<const float4*>(A + (size_t)k * RP + r);
-      const float4 b = *reinterpret_cast<const float4*>(B + (size_t)k * RP + r);
-      h0 = cmulc(make_float2(a.x, a.y), make_float2(b.x, b.y));
-      h1 = cmulc(make_float2(a.z, a.w), make_float2(b.z, b.w));
-      if (k > 0 && r == hc) {
-        const float2 h2 = cmulc(A[(size_t)k * RP + C0], B[(size_t)k * RP + C0]);
-        h0 = make_float2(0.5f * (h0.x + h2.x), 0.5f * (h0.y + h2.y));
+  // two rows per element: 16-byte loads along each (contiguous) column.  The
+  // regular columns (0 <= k < C1/2) load XC_UNR element pairs before using any,
+  // so that several loads per thread are in flight.
+  constexpr int NE = (C0 / 2) * XC_NBC;  // element pairs per CTA
+  constexpr int XC_UNR = 4;
+  for (int e0 = threadIdx.x; e0 < NE; e0 += T * XC_UNR) {
+    float4 av[XC_UNR], bv[XC_UNR];
+#pragma unroll
+    for (int u = 0; u < XC_UNR; u++) {
+      const int e = e0 + u * T;
+      av[u] = bv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (e < NE) {
+        const int c = e / (C0 / 2), r = 2 * (e - c * (C0 / 2));
+        const int k = k0 + c;
+        if (k < half) {
+          av[u] = __ldg(reinterpret_cast<const float4*>(A + (size_t)k * RP + r));
+          bv[u] = __ldg(reinterpret_cast<const float4*>(B + (size_t)k * RP + r));
+        }
       }
-    } else if (k == half) {
-      const float2* Ak = A + (size_t)k * RP;
-      const float2* Bk = B + (size_t)k * RP;
-      const int m0 = (r == 0) ? 0 : (r == hc ? C0 : C0 - r), m1 = C0 - r - 1;
-      h0 = cmulc(Bk[m0], Ak[m0]);  // conj(A) * B at the mirrored row
-      h1 = cmulc(Bk[m1], Ak[m1]);
     }
-    sm[c * LD + pidx(r)] = h0;
-    sm[c * LD + pidx(r + 1)] = h1;
+#pragma unroll
+    for (int u = 0; u < XC_UNR; u++) {
+      const int e = e0 + u * T;
+      if (e >= NE) continue;
+      const int c = e / (C0 / 2), r = 2 * (e - c * (C0 / 2));
+      const int k = k0 + c;
+      float2 h0 = make_float2(0.0f, 0.0f), h1 = h0;
+      if (k < half) {
+        h0 = cmulc(make_float2(av[u].x, av[u].y), make_float2(bv[u].x, bv[u].y));
+        h1 = cmulc(make_float2(av[u].z, av[u].w), make_float2(bv[u].z, bv[u].w));
+        if (k > 0 && r == hc) {
+          const float2 h2 = cmulc(A[(size_t)k * RP + C0], B[(size_t)k * RP + C0]);
+          h0 = make_float2(0.5f * (h0.x + h2.x), 0.5f * (h0.y + h2.y));
+        }
+      } else if (k == half) {
+        const float2* Ak = A + (size_t)k * RP;
+        const float2* Bk = B + (size_t)k * RP;
+        const int m0 = (r == 0) ? 0 : (r == hc ? C0 : C0 - r), m1 = C0 - r - 1;
+        h0 = cmulc(Bk[m0], Ak[m0]);  // conj(A) * B at the mirrored row
+        h1 = cmulc(Bk[m1], Ak[m1]);
+      }
+      sm[c * LD + pidx(r)] = h0;
+      sm[c * LD + pidx(r + 1)] = h1;
+    }
   }
   __syncthreads();
   block_fft<C0, XC_NBC, T, 1>(sm, tw);
