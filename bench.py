@@ -44,6 +44,13 @@ WORKLOADS = {
                attrs=dict(triMode="tri", shapePadded=[4096, 4096], fouCrop=[2048, 2048], maxShift=100,
                           pixelsize=0.105, voltage=300.0, filterMode="hot,dose", doseFiltParam=K2_DOSE,
                           subPixReg=16, shiftMethod="lanczos", Bmode="opti", doLazyFRC=True)),
+    # the K2 movie cut to 10 frames (142 MB of raw frames, still larger than L2): the case the
+    # per-kernel ncu captures run on
+    "k2x10": dict(movie=dict(n_frames=10, shape=(3838, 3710), seed=2024, mean_dose=0.8, drift_sigma=1.2,
+                             dtype="uint8", gain_map=True, hot_fraction=1e-4, hot_factor=50.0),
+                  attrs=dict(triMode="tri", shapePadded=[4096, 4096], fouCrop=[2048, 2048], maxShift=100,
+                             pixelsize=0.105, voltage=300.0, filterMode="hot,dose", doseFiltParam=K2_DOSE,
+                             subPixReg=16, shiftMethod="lanczos", Bmode="opti", doLazyFRC=True)),
     "small": dict(movie=dict(n_frames=20, shape=(1024, 1024), seed=1, mean_dose=1.0, drift_sigma=0.8),
                   attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[1024, 1024], maxShift=40,
                              pixelsize=0.1, voltage=300.0, filterMode="dose",
@@ -62,6 +69,33 @@ def algorithmic_bytes(N, H, W, C, w, M, b_in):
             "C_spectra": N * HW * b_in + 12 * HW + 2 * N * spec, "D_frame_terms": 2 * N * spec + 16 * N * w * w,
             "E_pairs": N * spec + 4 * M * w * w, "F_peaks": 4 * M * w * w, "G_shift_sum": N * HW * b_in + 24 * HW,
             "H_frc": 8 * HW, "I_dose": N * HW * b_in + 16 * HW}
+
+
+def fft_flops(N, P, C, w, M):
+    """Nominal FFT FLOPs per movie and stage, 5 n log2(n) per complex
+    transform of n points (a real transform counts half).  A pruned inverse
+    (columns at C, then only the w kept rows) costs (C/2 + 1 + w/2) column/row
+    transforms of length C."""
+    import math
+    full_real = 2.5 * P * P * math.log2(P * P)
+    pruned = (C // 2 + 1 + w // 2) * 5.0 * C * math.log2(C)
+    return {"C_spectra": 2 * N * full_real, "D_frame_terms": (4 * N + 1) * pruned, "E_pairs": M * pruned,
+            "I_dose": (N + 1) * full_real}
+
+
+def read_traffic():
+    """DRAM bytes per movie and stage measured by ncu (profiles/traffic.txt:
+    lines '<stage> <bytes>'), or {} when absent."""
+    out = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.txt")) as fh:
+            for ln in fh:
+                p = ln.split("#", 1)[0].split()
+                if len(p) >= 2:
+                    out[p[0]] = int(float(p[1]))
+    except OSError:
+        pass
+    return out
 
 
 def measured_peaks():
@@ -297,6 +331,8 @@ def main():
     dev_ms = ev0.elapsed_time(ev1)
     stage_ms = eng.stage_ms()
     eng.profile = None
+    if args.profile_only:
+        return
     t_step = max(dev_ms / 1000.0, 1e-9) / args.steps
     if dist is not None:
         tt = torch.tensor([t_step], device=dev)
@@ -352,17 +388,19 @@ def main():
     dom = max(per_step, key=per_step.get)
     peak, peak_kind = measured_peaks()
     achieved = ab[dom] / (per_step[dom] / 1000.0) / 1e9
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
-            traffic = json.load(fh).get(dom)
-    except Exception:
-        pass
+    traffic = read_traffic().get(dom) if args.workload == "k2" else None
+    P = int(wl["attrs"]["shapePadded"][0])
+    fl = fft_flops(N, P, C, w, M if M is not None else N - 1)
+    # FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 FLOP x SM clock
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind,
             "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+            "traffic_gbs": round(traffic / (per_step[dom] / 1000.0) / 1e9, 1) if traffic else None,
             "algorithmic_bytes": ab[dom], "stage_ms_per_step": {k: round(v, 3) for k, v in sorted(per_step.items())},
             "movie_algorithmic_bytes": sum(ab.values()),
-            "movie_frac": round(sum(ab.values()) / t_step / 1e9 / peak, 4)}
+            "movie_frac": round(sum(ab.values()) / t_step / 1e9 / peak, 4),
+            "fft_tflops": {k: round(v / (per_step[k] / 1000.0) / 1e12, 2) for k, v in fl.items() if k in per_step},
+            "fp32_peak_tflops": round(fp32_peak, 1)}
 
     # ---- accuracy on this movie vs the known drift (the float64 oracle comparison is in the tests)
     tr = np.asarray(last.translations)
