@@ -180,6 +180,26 @@ int zr_xcorr_terms(const void* G, const void* S, const void* GM, int N, int C0, 
 int zr_xcorr_pairs(const void* G, const float* terms, const int* pairs, int M, int N, int C0, int C1,
                    int max_shift, float* cwin, void* work, size_t work_bytes, void* stream);
 
+/* zr_xcorr_pairs without a work buffer.  This entry point has no counterpart
+ * in the reference.  It is for callers that may not allocate device memory
+ * when they call in: a host process that owns the whole device-memory budget
+ * and forbids allocation inside its callbacks, or a caller that keeps every
+ * allocation out of its per-request loop.  The scratch is a device array of
+ * ZR_XCORR_STATIC_SCRATCH bytes compiled into the library; the pairs run in
+ * waves of floor(ZR_XCORR_STATIC_SCRATCH / (2*max_shift * K4 * 8)) pairs
+ * (K4 = zr_spectrum_pitch(C1)), and a size whose single pair does not fit
+ * returns ZR_ESIZE.  Nothing in the scratch has to start at zero.
+ * - The first call on each device looks the array's address up
+ *   (cudaGetSymbolAddress, with that device current); make that first call
+ *   before any stream capture on the device.
+ * - Every call on a device shares the one array: calls that overlap in time
+ *   (different streams or threads with no ordering between them) race on it
+ *   and give wrong results.  Order them on one stream.
+ * Results are those of zr_xcorr_pairs. */
+#define ZR_XCORR_STATIC_SCRATCH (16u << 20)
+int zr_xcorr_pairs_noalloc(const void* G, const float* terms, const int* pairs, int M, int N, int C0, int C1,
+                           int max_shift, float* cwin, void* stream);
+
 /* ---- peak search: locatePeak, zorro.py:1099-1231 ---- */
 int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr_peak_params_t* params,
                     zr_peak_result_t* results, void* stream);
