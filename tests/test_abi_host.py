@@ -116,3 +116,27 @@ def test_numpy_axis0_sum_is_sequential():
     for k in range(40):
         s = s + a[k]
     assert np.array_equal(np.sum(a, axis=0), s)
+
+
+def test_logistic_fit_matches_scipy_nelder_mead():
+    """The product's Nelder-Mead returns scipy's point bit for bit on the
+    logistic-CDF objective (ties and small bin counts included)."""
+    import scipy.optimize
+    rng = np.random.default_rng(5)
+    for trial in range(40):
+        n = int(rng.choice([15, 28, 45, 190, 780]))
+        ps = np.abs(rng.normal(rng.uniform(5, 40), rng.uniform(1, 10), n)) + 0.01
+        if trial % 5 == 0:
+            ps = np.round(ps)
+        pdf, edges = np.histogram(ps, bins=int(ps.size / 7.0))
+        h = edges[:-1]
+        cdf = np.cumsum(pdf.astype("float32"))
+        cdf /= cdf[-1]
+        with np.errstate(over="ignore"):
+            r = scipy.optimize.minimize(zo._logistic_cdf_error64, (np.mean(ps), 5.0, 1.0), args=(h, cdf),
+                                        method="Nelder-Mead", bounds=((np.min(ps), np.max(ps)), (0.1, 20.0), (0.05, 5.0)),
+                                        options={"xatol": 1e-10, "fatol": 1e-14, "maxiter": 4000, "maxfev": 8000})
+            x, fv, nfev = hm.nelder_mead_bounded(hm._logistic_objective(h, cdf), (np.mean(ps), 5.0, 1.0),
+                                                 (float(np.min(ps)), 0.1, 0.05), (float(np.max(ps)), 20.0, 5.0),
+                                                 1e-10, 1e-14, 4000, 8000)
+        assert np.array_equal(x, r.x) and fv == r.fun and nfev == r.nfev, (trial, x, r.x)

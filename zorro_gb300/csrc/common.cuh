@@ -98,6 +98,66 @@ __device__ __forceinline__ float4 load4_corrected(const FrameSrc& f, int n, long
   return v;
 }
 
+// load4_corrected split in two, so that a thread can issue the loads of
+// several pixel quads before it uses any: Px4 holds the raw bits and the map
+// values of one quad; finish4 applies the same operations in the same order.
+struct Px4 {
+  uint4 raw;  // the quad's raw bits: u8 in .x, u16/f16 in .x/.y, f32 in .x-.w
+  float4 g, a, b;
+};
+
+__device__ __forceinline__ void fetch4(const FrameSrc& f, int n, long long p, Px4& q) {
+  const long long i = (long long)n * f.fstride + p;
+  switch (f.type) {
+    case ZR_U8: q.raw.x = __ldg(reinterpret_cast<const unsigned int*>((const uint8_t*)f.raw + i)); break;
+    case ZR_U16:
+    case ZR_F16: {
+      const uint2 r = __ldg(reinterpret_cast<const uint2*>((const uint16_t*)f.raw + i));
+      q.raw.x = r.x;
+      q.raw.y = r.y;
+      break;
+    }
+    default: q.raw = __ldg(reinterpret_cast<const uint4*>((const float*)f.raw + i));
+  }
+  if (f.gain) q.g = __ldg(reinterpret_cast<const float4*>(f.gain + p));
+  if (f.ha) {
+    q.a = __ldg(reinterpret_cast<const float4*>(f.ha + p));
+    q.b = __ldg(reinterpret_cast<const float4*>(f.hb + p));
+  }
+}
+
+__device__ __forceinline__ float4 finish4(const FrameSrc& f, const Px4& q) {
+  float4 v;
+  switch (f.type) {
+    case ZR_U8: {
+      const unsigned int r = q.raw.x;
+      v = make_float4((float)(r & 0xffu), (float)((r >> 8) & 0xffu), (float)((r >> 16) & 0xffu), (float)(r >> 24));
+      break;
+    }
+    case ZR_U16:
+      v = make_float4((float)(q.raw.x & 0xffffu), (float)(q.raw.x >> 16), (float)(q.raw.y & 0xffffu),
+                      (float)(q.raw.y >> 16));
+      break;
+    case ZR_F16:
+      v = make_float4(__half2float(__ushort_as_half((unsigned short)(q.raw.x & 0xffffu))),
+                      __half2float(__ushort_as_half((unsigned short)(q.raw.x >> 16))),
+                      __half2float(__ushort_as_half((unsigned short)(q.raw.y & 0xffffu))),
+                      __half2float(__ushort_as_half((unsigned short)(q.raw.y >> 16))));
+      break;
+    default:
+      v = make_float4(__uint_as_float(q.raw.x), __uint_as_float(q.raw.y), __uint_as_float(q.raw.z),
+                      __uint_as_float(q.raw.w));
+  }
+  if (f.gain)
+    v = make_float4(__fmul_rn(q.g.x, v.x), __fmul_rn(q.g.y, v.y), __fmul_rn(q.g.z, v.z), __fmul_rn(q.g.w, v.w));
+  if (f.gdiv != 0.0f)
+    v = make_float4(__fdiv_rn(v.x, f.gdiv), __fdiv_rn(v.y, f.gdiv), __fdiv_rn(v.z, f.gdiv), __fdiv_rn(v.w, f.gdiv));
+  if (f.ha)
+    v = make_float4(__fmaf_rn(q.a.x, v.x, q.b.x), __fmaf_rn(q.a.y, v.y, q.b.y), __fmaf_rn(q.a.z, v.z, q.b.z),
+                    __fmaf_rn(q.a.w, v.w, q.b.w));
+  return v;
+}
+
 __device__ __forceinline__ int ilog2c(int v) { return 31 - __clz(v); }
 
 }  // namespace zr

@@ -108,14 +108,29 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
       const float2* src = s + b * LD;
       const int k = j & (NS - 1);
 #pragma unroll
-      for (int r = 0; r < R; r++) {
-        float2 x = src[pidx(j + r * LR)];
-        if (NS > 1 && r > 0) {
-          float2 w = __ldg(tw + k * r * TWS);
-          if (DIR > 0) w.y = -w.y;
-          x = cmul(x, w);
+      for (int r = 0; r < R; r++) v[i][r] = src[pidx(j + r * LR)];
+      if (NS > 1) {
+        // W^(k r) for r = 1 .. R-1: the powers 1, 2, 4 from the table, the
+        // others as products of two of them (one extra rounding), which
+        // keeps the load/store pipe for the data
+        float2 w[R];
+        w[1] = __ldg(tw + k * TWS);
+        if constexpr (R >= 4) {
+          w[2] = __ldg(tw + 2 * k * TWS);
+          w[3] = cmul(w[1], w[2]);
         }
-        v[i][r] = x;
+        if constexpr (R == 8) {
+          w[4] = __ldg(tw + 4 * k * TWS);
+          w[5] = cmul(w[1], w[4]);
+          w[6] = cmul(w[2], w[4]);
+          w[7] = cmul(w[3], w[4]);
+        }
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+          float2 ww = w[r];
+          if (DIR > 0) ww.y = -ww.y;
+          v[i][r] = cmul(v[i][r], ww);
+        }
       }
       dft<R, DIR>(v[i]);
     }

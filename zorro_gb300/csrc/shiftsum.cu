@@ -27,24 +27,42 @@ __global__ void __launch_bounds__(SS_THR)
 #pragma unroll
   for (int i = 0; i < RPT; i++) s[i] = se[i] = so[i] = 0.0f;
   const int H = f.H, W = f.W;
+  // the halo tile of frame n+1 is loaded into registers while frame n is
+  // filtered, so that its loads overlap the arithmetic and the stores
+  constexpr int TE = (SS_TY + 2) * (SS_TX + 2);
+  constexpr int LPT = (TE + SS_THR - 1) / SS_THR;
+  float pre[LPT];
+  auto fetch = [&](int n) {
+    const zr_shift_t t = sh[n];
+#pragma unroll
+    for (int l = 0; l < LPT; l++) {
+      const int e = threadIdx.x + l * SS_THR;
+      pre[l] = 0.0f;
+      if (e < TE) {
+        const int i = e / (SS_TX + 2), j = e - i * (SS_TX + 2);
+        if (y0 - 1 + i < H + 1 && x0 - 1 + j < W + 1) {
+          const int Y = refl1(y0 - 1 + i, H), X = refl1(x0 - 1 + j, W);
+          // roll offsets arrive reduced to [0, H) and [0, W)
+          int sy = Y - t.roll_y;
+          if (sy < 0) sy += H;
+          int sx = X - t.roll_x;
+          if (sx < 0) sx += W;
+          pre[l] = load_corrected(f, n, sy, sx);
+        }
+      }
+    }
+  };
+  fetch(0);
   for (int n = 0; n < f.N; n++) {
     const zr_shift_t t = sh[n];
     __syncthreads();
-    for (int e = threadIdx.x; e < (SS_TY + 2) * (SS_TX + 2); e += SS_THR) {
-      const int i = e / (SS_TX + 2), j = e - i * (SS_TX + 2);
-      const int Y = refl1(y0 - 1 + i, H), X = refl1(x0 - 1 + j, W);
-      float v = 0.0f;
-      if (y0 - 1 + i < H + 1 && x0 - 1 + j < W + 1) {
-        // roll offsets arrive reduced to [0, H) and [0, W)
-        int sy = Y - t.roll_y;
-        if (sy < 0) sy += H;
-        int sx = X - t.roll_x;
-        if (sx < 0) sx += W;
-        v = load_corrected(f, n, sy, sx);
-      }
-      tile[i][j] = v;
+#pragma unroll
+    for (int l = 0; l < LPT; l++) {
+      const int e = threadIdx.x + l * SS_THR;
+      if (e < TE) tile[e / (SS_TX + 2)][e % (SS_TX + 2)] = pre[l];
     }
     __syncthreads();
+    if (n + 1 < f.N) fetch(n + 1);
     const int x = x0 + tx;
 #pragma unroll
     for (int i = 0; i < RPT; i++) {

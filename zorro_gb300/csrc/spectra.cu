@@ -36,30 +36,63 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
   if (mode == 0 && !mask && (f.fstride & 3) == 0) {
     // 4 pixels per thread and step: aligned vector loads of the raw frame and
     // every map; the unaligned head (< 4 pixels) and tail go pixel by pixel
-    for (int e = threadIdx.x; e < NBR * (P1 / 4); e += T) {
-      const int r = e / (P1 / 4), q = e - r * (P1 / 4);
-      const int y = g * NBR + r;
-      float2* srow = sm + r * LD;
-      if (y >= rows) {
+    // FR_UNR quads per thread are fetched before any is used, so that several
+    // loads per thread are in flight
+    constexpr int NQ = NBR * (P1 / 4);
+    constexpr int FR_UNR = 4;
+    for (int e0 = threadIdx.x; e0 < NQ; e0 += T * FR_UNR) {
+      Px4 px[FR_UNR];
 #pragma unroll
-        for (int j = 0; j < 4; j++) srow[pidx(4 * q + j)] = make_float2(0.0f, 0.0f);
-        continue;
+      for (int u = 0; u < FR_UNR; u++) {
+        const int e = e0 + u * T;
+        if (e < NQ) {
+          const int r = e / (P1 / 4), q = e - r * (P1 / 4);
+          const int y = g * NBR + r;
+          if (y < rows) {
+            const long long p0 = (long long)y * f.W;
+            const int x = (int)((4 - (p0 & 3)) & 3) + 4 * q;
+            if (x + 3 < cols) fetch4(f, n, p0 + x, px[u]);
+          }
+        }
       }
-      const long long p0 = (long long)y * f.W;
-      const int off = (int)((4 - (p0 & 3)) & 3);  // first x with (p0 + x) % 4 == 0
-      const int x = off + 4 * q;
-      if (x + 3 < cols) {
-        const float4 v = load4_corrected(f, n, p0 + x);
-        const float u0 = v.x - mu, u1 = v.y - mu, u2 = v.z - mu, u3 = v.w - mu;
-        srow[pidx(x)] = make_float2(u0, u0 * u0);
-        srow[pidx(x + 1)] = make_float2(u1, u1 * u1);
-        srow[pidx(x + 2)] = make_float2(u2, u2 * u2);
-        srow[pidx(x + 3)] = make_float2(u3, u3 * u3);
-      } else {
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int xx = x + j;
-          if (xx < P1) {
+      for (int u = 0; u < FR_UNR; u++) {
+        const int e = e0 + u * T;
+        if (e >= NQ) continue;
+        const int r = e / (P1 / 4), q = e - r * (P1 / 4);
+        const int y = g * NBR + r;
+        float2* srow = sm + r * LD;
+        if (y >= rows) {
+#pragma unroll
+          for (int j = 0; j < 4; j++) srow[pidx(4 * q + j)] = make_float2(0.0f, 0.0f);
+          continue;
+        }
+        const long long p0 = (long long)y * f.W;
+        const int off = (int)((4 - (p0 & 3)) & 3);  // first x with (p0 + x) % 4 == 0
+        const int x = off + 4 * q;
+        if (x + 3 < cols) {
+          const float4 v = finish4(f, px[u]);
+          const float u0 = v.x - mu, u1 = v.y - mu, u2 = v.z - mu, u3 = v.w - mu;
+          srow[pidx(x)] = make_float2(u0, u0 * u0);
+          srow[pidx(x + 1)] = make_float2(u1, u1 * u1);
+          srow[pidx(x + 2)] = make_float2(u2, u2 * u2);
+          srow[pidx(x + 3)] = make_float2(u3, u3 * u3);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const int xx = x + j;
+            if (xx < P1) {
+              float2 z = make_float2(0.0f, 0.0f);
+              if (xx < cols) {
+                const float u = load_corrected(f, n, y, xx) - mu;
+                z = make_float2(u, u * u);
+              }
+              srow[pidx(xx)] = z;
+            }
+          }
+        }
+        if (q == 0) {
+          for (int xx = 0; xx < off; xx++) {
             float2 z = make_float2(0.0f, 0.0f);
             if (xx < cols) {
               const float u = load_corrected(f, n, y, xx) - mu;
@@ -67,16 +100,6 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
             }
             srow[pidx(xx)] = z;
           }
-        }
-      }
-      if (q == 0) {
-        for (int xx = 0; xx < off; xx++) {
-          float2 z = make_float2(0.0f, 0.0f);
-          if (xx < cols) {
-            const float u = load_corrected(f, n, y, xx) - mu;
-            z = make_float2(u, u * u);
-          }
-          srow[pidx(xx)] = z;
         }
       }
     }
