@@ -145,7 +145,8 @@ int zr_hotpix_maps(const float* unaligned_sum, int height, int width, int n_fram
 
 /* sums[n] (double, accumulated) += sum of the corrected frame n over
  * [0,H)x[0,W).  Used to subtract each frame's mean before the transform
- * (an exact identity of the masked correlation, see DESIGN). */
+ * (the masked normalised correlation with a binary mask does not change when
+ * a constant is subtracted inside the mask). */
 int zr_frame_sums(const zr_frames_t* frames, double* sums, void* stream);
 
 int zr_spectrum_pitch(int C1);
@@ -232,6 +233,18 @@ int zr_tiled_frc(const float* even, const float* odd, int height, int width, int
  * problem instead). */
 int zr_l1_solve(const double* A, const double* b, const double* w, int m, int n, double lo, double hi,
                 double* x, int* status);
+
+/* Logistic fit of the peak-significance CDF: the minimisation in
+ * cdfLogisticCurve (zorro.py:1981-2022) of the error of zorro_util.py:862-863,
+ * sum_i |cdf_i - (1 - 1/(1 + exp(-x1 (x0 - h_i)))^x2)|, over the box
+ * [lo, hi].  The reference minimises it with unseeded basinhopping
+ * (zorro.py:2008); this is a deterministic bounded Nelder-Mead (the
+ * coefficients, start simplex and stopping tests of scipy's 'Nelder-Mead'
+ * with bounds) from x0.  Host code; x_out[3], *f_out (may be null) and
+ * *n_eval (may be null) receive the point, its value and the evaluations. */
+int zr_logistic_fit(const double* h_sigma, const float* cdf, int nbins, const double* x0, const double* lo,
+                    const double* hi, double xatol, double fatol, int maxiter, int maxfev, double* x_out,
+                    double* f_out, int* n_eval);
 
 /* ---- dose filter: doseFilter, zorro.py:2349-2494 ---- */
 

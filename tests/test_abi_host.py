@@ -118,12 +118,26 @@ def test_numpy_axis0_sum_is_sequential():
     assert np.array_equal(np.sum(a, axis=0), s)
 
 
+def _numpy_exp_pow_are_libm():
+    import math
+    rng = np.random.default_rng(2)
+    x = rng.uniform(-700, 700, 20000)
+    v, e = rng.uniform(1, 1e6, 20000), rng.uniform(0.05, 5, 20000)
+    return (np.array_equal(np.exp(x), [math.exp(t) for t in x]) and
+            np.array_equal(v ** e, [math.pow(a, b) for a, b in zip(v, e)]))
+
+
 def test_logistic_fit_matches_scipy_nelder_mead():
-    """The product's Nelder-Mead returns scipy's point bit for bit on the
-    logistic-CDF objective (ties and small bin counts included)."""
+    """zr_logistic_fit returns scipy's Nelder-Mead point bit for bit on the
+    logistic-CDF objective (ties and small bin counts included) where NumPy's
+    exp and pow are the C library's (aarch64); NumPy's SIMD exp/pow on x86
+    differ in the last bit for a few percent of arguments, which moves the
+    simplex path."""
     import scipy.optimize
+    if not _numpy_exp_pow_are_libm():
+        pytest.skip("NumPy's exp/pow are not the C library's on this platform")
     rng = np.random.default_rng(5)
-    for trial in range(40):
+    for trial in range(60):
         n = int(rng.choice([15, 28, 45, 190, 780]))
         ps = np.abs(rng.normal(rng.uniform(5, 40), rng.uniform(1, 10), n)) + 0.01
         if trial % 5 == 0:
@@ -136,7 +150,26 @@ def test_logistic_fit_matches_scipy_nelder_mead():
             r = scipy.optimize.minimize(zo._logistic_cdf_error64, (np.mean(ps), 5.0, 1.0), args=(h, cdf),
                                         method="Nelder-Mead", bounds=((np.min(ps), np.max(ps)), (0.1, 20.0), (0.05, 5.0)),
                                         options={"xatol": 1e-10, "fatol": 1e-14, "maxiter": 4000, "maxfev": 8000})
-            x, fv, nfev = hm.nelder_mead_bounded(hm._logistic_objective(h, cdf), (np.mean(ps), 5.0, 1.0),
-                                                 (float(np.min(ps)), 0.1, 0.05), (float(np.max(ps)), 20.0, 5.0),
-                                                 1e-10, 1e-14, 4000, 8000)
-        assert np.array_equal(x, r.x) and fv == r.fun and nfev == r.nfev, (trial, x, r.x)
+        x = hm.logistic_nelder_mead(h, cdf, (np.mean(ps), 5.0, 1.0), (np.min(ps), 0.1, 0.05), (np.max(ps), 20.0, 5.0))
+        assert np.array_equal(x, r.x), (trial, x, r.x)
+
+
+def test_logistic_fit_converges_to_a_minimum():
+    """On every platform: the native fit ends on a point whose objective is
+    no worse than scipy's by more than the stopping tolerance on well-posed
+    problems (hundreds of peaks)."""
+    import scipy.optimize
+    rng = np.random.default_rng(9)
+    for trial in range(10):
+        ps = np.abs(rng.normal(rng.uniform(10, 40), rng.uniform(2, 8), 780)) + 0.01
+        pdf, edges = np.histogram(ps, bins=int(ps.size / 7.0))
+        h = edges[:-1]
+        cdf = np.cumsum(pdf.astype("float32"))
+        cdf /= cdf[-1]
+        x = hm.logistic_nelder_mead(h, cdf, (np.mean(ps), 5.0, 1.0), (np.min(ps), 0.1, 0.05), (np.max(ps), 20.0, 5.0))
+        with np.errstate(over="ignore"):
+            r = scipy.optimize.minimize(zo._logistic_cdf_error64, (np.mean(ps), 5.0, 1.0), args=(h, cdf),
+                                        method="Nelder-Mead", bounds=((np.min(ps), np.max(ps)), (0.1, 20.0), (0.05, 5.0)),
+                                        options={"xatol": 1e-10, "fatol": 1e-14, "maxiter": 4000, "maxfev": 8000})
+            fx = zo._logistic_cdf_error64(x, h, cdf)
+        assert fx <= r.fun * (1 + 1e-6) + 1e-9, (trial, fx, r.fun)

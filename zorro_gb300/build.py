@@ -23,8 +23,11 @@ BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libzorrogb.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-O3"]
+# Host code is compiled without multiply-add contraction: the host solves
+# (drift solve, logistic fit) then round the same way on aarch64 (where GCC
+# would otherwise fuse a*b+c) as on x86.  Device code keeps nvcc's default.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
 
 def nvcc_path():

@@ -2,12 +2,13 @@
 //
 // A CTA transforms NB sequences of length L (a power of two, 2..8192) that sit
 // in shared memory.  Element i of sequence b lives at s[b*ld(L) + pidx(i)]:
-// one padding slot every 8 elements keeps the radix-8 scatter of the first
+// one padding slot every 16 elements keeps the radix-16 scatter of the first
 // pass free of bank conflicts, and the row pitch (ld_of) keeps tiles of 4
-// sequences x 4 elements conflict-free.  Each pass is a radix-8 (the last pass radix 2
-// or 4 when log2(L) is not a multiple of 3) Stockham step: every thread reads
-// its butterflies' inputs into registers, the CTA synchronises, and the
-// outputs are written back in place.  No ping-pong buffer is needed.
+// sequences x 4 elements conflict-free.  Each pass is a radix-16 Stockham
+// step (the last pass radix 2, 4 or 8 when log2(L) is not a multiple of 4):
+// every thread reads its butterflies' inputs into registers, the CTA
+// synchronises, and the outputs are written back in place.  No ping-pong
+// buffer is needed.
 //
 // Twiddles come from a table of W_8192^k = exp(-2 pi i k / 8192) computed in
 // double precision on the host and rounded to float (``tw`` argument).
@@ -20,12 +21,12 @@ namespace zr {
 
 constexpr int TWN = 8192;  // twiddle table length
 
-__host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 3); }
+__host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 4); }
 // Row pitch of one sequence: the padded length rounded so that pitch = 4
 // (mod 16) float2s; then 4 sequences x 4 consecutive elements (the tile the
 // row/column passes move per half-warp) fall on 32 distinct banks.
 __host__ __device__ __forceinline__ constexpr int ld_of(int L) {
-  return (((L + (L >> 3)) + 15) & ~15) + 4;
+  return (((L + (L >> 4)) + 15) & ~15) + 4;
 }
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -89,11 +90,49 @@ __device__ __forceinline__ void dft<8, -1>(float2* x) { dft8<-1>(x); }
 template <>
 __device__ __forceinline__ void dft<8, 1>(float2* x) { dft8<1>(x); }
 
+// 16-point DFT as 4 x 4: length-4 DFTs over n1 (n = 4 n1 + n2), the twiddles
+// W16^(n2 k1), length-4 DFTs over n2; output k = k1 + 4 k2.
+template <int DIR>
+__device__ __forceinline__ void dft16(float2* x) {
+  const float c1 = 0.92387953251128675613f;  // cos(pi/8)
+  const float s1 = 0.38268343236508977173f;  // sin(pi/8)
+  const float h = 0.70710678118654752440f;
+#pragma unroll
+  for (int n2 = 0; n2 < 4; n2++) dft4<DIR>(x[n2], x[4 + n2], x[8 + n2], x[12 + n2]);
+  // x[4 k1 + n2] now holds Y_{n2}[k1]; multiply by W16^(DIR' n2 k1), where
+  // W16^m = exp(DIR * 2 pi i m / 16)
+  auto tw = [&](float2 v, float cr, float si) {  // v * (cr + DIR*i*si)
+    return make_float2(v.x * cr - DIR * v.y * si, v.y * cr + DIR * v.x * si);
+  };
+  x[5] = tw(x[5], c1, s1);     // m = 1
+  x[6] = tw(x[6], h, h);       // m = 2
+  x[7] = tw(x[7], s1, c1);     // m = 3
+  x[9] = tw(x[9], h, h);       // m = 2
+  x[10] = mul_si<DIR>(x[10]);  // m = 4
+  x[11] = tw(x[11], -h, h);    // m = 6
+  x[13] = tw(x[13], s1, c1);   // m = 3
+  x[14] = tw(x[14], -h, h);    // m = 6
+  x[15] = tw(x[15], -c1, -s1); // m = 9
+  float2 y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    float2 a = x[4 * k1], b = x[4 * k1 + 1], c = x[4 * k1 + 2], d = x[4 * k1 + 3];
+    dft4<DIR>(a, b, c, d);
+    y[k1] = a; y[k1 + 4] = b; y[k1 + 8] = c; y[k1 + 12] = d;
+  }
+#pragma unroll
+  for (int k = 0; k < 16; k++) x[k] = y[k];
+}
+template <>
+__device__ __forceinline__ void dft<16, -1>(float2* x) { dft16<-1>(x); }
+template <>
+__device__ __forceinline__ void dft<16, 1>(float2* x) { dft16<1>(x); }
+
 // One Stockham pass (radix R, NS = product of the radices already applied),
 // then the remaining passes.
 template <int L, int NB, int T, int DIR, int NS>
 __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ tw) {
-  constexpr int R = (L / NS >= 8) ? 8 : (L / NS);
+  constexpr int R = (L / NS >= 16) ? 16 : (L / NS);
   constexpr int LR = L / R;
   constexpr int NBF = NB * LR;
   constexpr int K = (NBF + T - 1) / T;
@@ -110,26 +149,30 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
 #pragma unroll
       for (int r = 0; r < R; r++) v[i][r] = src[pidx(j + r * LR)];
       if (NS > 1) {
-        // W^(k r) for r = 1 .. R-1: the powers 1, 2, 4 from the table, the
-        // others as products of two of them (one extra rounding), which
-        // keeps the load/store pipe for the data
-        float2 w[R];
-        w[1] = __ldg(tw + k * TWS);
-        if constexpr (R >= 4) {
-          w[2] = __ldg(tw + 2 * k * TWS);
-          w[3] = cmul(w[1], w[2]);
-        }
-        if constexpr (R == 8) {
-          w[4] = __ldg(tw + 4 * k * TWS);
-          w[5] = cmul(w[1], w[4]);
-          w[6] = cmul(w[2], w[4]);
-          w[7] = cmul(w[3], w[4]);
-        }
-#pragma unroll
-        for (int r = 1; r < R; r++) {
-          float2 ww = w[r];
+        // W^(k r) for r = 1 .. R-1: a few powers from the table, the others
+        // as products of two table values (one extra rounding), which keeps
+        // the load/store pipe for the data
+        auto twiddle = [&](int r, float2 ww) {
           if (DIR > 0) ww.y = -ww.y;
           v[i][r] = cmul(v[i][r], ww);
+        };
+        const float2 w1 = __ldg(tw + k * TWS);
+        if constexpr (R == 2) {
+          twiddle(1, w1);
+        } else {
+          const float2 w2 = __ldg(tw + 2 * k * TWS);
+          const float2 w3 = (R == 16) ? __ldg(tw + 3 * k * TWS) : cmul(w1, w2);
+          twiddle(1, w1);
+          twiddle(2, w2);
+          twiddle(3, w3);
+#pragma unroll
+          for (int a = 4; a < R; a += 4) {
+            const float2 wa = __ldg(tw + a * k * TWS);
+            twiddle(a, wa);
+            twiddle(a + 1, cmul(R == 16 ? wa : w1, R == 16 ? w1 : wa));
+            twiddle(a + 2, cmul(w2, wa));
+            twiddle(a + 3, cmul(w3, wa));
+          }
         }
       }
       dft<R, DIR>(v[i]);

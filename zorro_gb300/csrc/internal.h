@@ -26,10 +26,10 @@ inline int ilog2(long long v) {
 #define ZR_FFT_EPT 32
 #endif
 #ifndef ZR_FFT_MINB
-#define ZR_FFT_MINB 1
+#define ZR_FFT_MINB 2
 #endif
-constexpr int fft_threads(int L, int NB) {
-  return (NB * L / ZR_FFT_EPT < 64) ? 64 : ((NB * L / ZR_FFT_EPT > 512) ? 512 : NB * L / ZR_FFT_EPT);
+constexpr int fft_threads(int L, int NB, int ept = ZR_FFT_EPT) {
+  return (NB * L / ept < 64) ? 64 : ((NB * L / ept > 512) ? 512 : NB * L / ept);
 }
 // Resident CTAs per SM to ask the register allocator for (short transforms).
 constexpr int fft_minblocks(int L) { return L <= 2048 ? ZR_FFT_MINB : 1; }

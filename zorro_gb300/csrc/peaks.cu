@@ -31,6 +31,7 @@ constexpr int PK_MAXR = 64;    // largest filter radius
 constexpr int PK_SUBR = 8;     // +/- patch half-size (zorro.py:619)
 
 struct PkShared {
+  double gw[2 * PK_MAXR + 1];
   float wy[2 * PK_MAXR + 1];
   float wx[2 * PK_MAXR + 1];
   double red[PK_T / 32][3];
@@ -49,19 +50,30 @@ __device__ __forceinline__ int reflect_idx(int i, int n) {
 }
 
 // Gaussian weights exp(-0.5 k^2 / sigma^2), normalised (double, then float).
-__device__ int gauss_weights(double sigma, float* w) {
+// Every thread computes some of the exponentials; thread 0 sums them in
+// order.  All threads must call (with the same sigma).
+__device__ int gauss_weights(double sigma, float* w, PkShared& sh) {
   if (!(sigma > 1e-15)) {
     if (threadIdx.x == 0) w[0] = 1.0f;
     return 0;
   }
   int r = (int)(4.0 * sigma + 0.5);
   if (r > PK_MAXR) r = PK_MAXR;
-  if (threadIdx.x == 0) {
-    const double c = -0.5 / (sigma * sigma);
-    double s = 0.0;
-    for (int k = -r; k <= r; k++) s += exp(c * (double)k * (double)k);
-    for (int k = -r; k <= r; k++) w[k + r] = (float)(exp(c * (double)k * (double)k) / s);
+  const double c = -0.5 / (sigma * sigma);
+  __syncthreads();  // a previous call may still be reading sh.gw
+  for (int i = threadIdx.x; i <= 2 * r; i += blockDim.x) {
+    const int k = i - r;
+    sh.gw[i] = exp(c * (double)k * (double)k);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i <= 2 * r; i++) s += sh.gw[i];
+    sh.bc[0] = s;
+  }
+  __syncthreads();
+  const double s = sh.bc[0];
+  for (int i = threadIdx.x; i <= 2 * r; i += blockDim.x) w[i] = (float)(sh.gw[i] / s);
   return r;
 }
 
@@ -208,70 +220,135 @@ __device__ void filter_pass(const float* C, float* V, const int* rtab, int w, in
 // The same visit for w % 4 == 0 with the work vectorised: each thread
 // filters 4 consecutive columns; the vertical taps are float4 loads, the
 // horizontal taps slide a 4-wide register window one column at a time.
-template <int MODE>
+// Rows per thread of the vectorised filter pass (register blocking of the
+// vertical pass): 4 while the window, the row block and the static shared
+// memory fit in one SM's shared memory, else 2.
+__host__ __device__ constexpr int pk_vec_rows(int w) { return w <= 216 ? 4 : 2; }
+__host__ __device__ constexpr int pk_vec_pitch(int w) { return w + 8; }
+
+// Horizontal pass of one row for 4 consecutive outputs x0..x0+3 away from
+// the borders: 16-byte loads of the row (p = row + x0 - rx - OFF is 16-byte
+// aligned), taps in order, the same fused multiply-adds as the scalar form.
+template <int OFF>
+__device__ __forceinline__ void hrow4(const float* __restrict__ p, const float* __restrict__ wx, int rx, float& f0,
+                                      float& f1, float& f2, float& f3) {
+  float4 A = *reinterpret_cast<const float4*>(p), B = *reinterpret_cast<const float4*>(p + 4);
+  for (int k0 = 0; k0 <= 2 * rx; k0 += 4) {
+    const float4 Cn = *reinterpret_cast<const float4*>(p + k0 + 8);
+    const float s[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, Cn.x, Cn.y, Cn.z, Cn.w};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      if (k0 + q <= 2 * rx) {
+        const float wk = wx[k0 + q];
+        f0 = fmaf(wk, s[OFF + q], f0);
+        f1 = fmaf(wk, s[OFF + q + 1], f1);
+        f2 = fmaf(wk, s[OFF + q + 2], f2);
+        f3 = fmaf(wk, s[OFF + q + 3], f3);
+      }
+    }
+    A = B;
+    B = Cn;
+  }
+}
+
+// Vectorised form for w % 4 == 0: w/4 column lanes of 4 columns, RB lanes of
+// R rows each per block of RB*R rows.  The vertical pass slides over the
+// input rows once per thread (R outputs share each 16-byte row load), the
+// horizontal pass reads 16-byte chunks of the filtered rows; every output
+// still accumulates its taps in order with fmaf, as the scalar form does.
+template <int MODE, int R>
 __device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx,
                              const float* wy, const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st,
                              float& amax, int& aidx) {
-  // w/4 column lanes (each 4 columns wide) x RB rows of a block
   const int w4 = w >> 2;
   const int RB = PK_T / w4;
+  const int VP = pk_vec_pitch(w);
   const int tx = threadIdx.x % w4, ty = threadIdx.x / w4;
+  const int x0 = tx << 2;
   float s1 = 0.0f, s2 = 0.0f, mx = -INFINITY;
   float bv = -INFINITY;
   int bi = 0x7fffffff;
   int cnt = 0;
-  for (int y0 = 0; y0 < w; y0 += RB) {
-    const int y = y0 + ty;
-    if (y < w && ty < RB) {
-      const int x0 = tx << 2;
-      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      const bool interior = (y >= ry && y + ry < w);
-      const float* p = C + (y - ry) * w + x0;
+  const int OFF = (-rx) & 3;
+  const bool xin = (x0 >= rx && x0 + 3 + rx < w);
+  for (int yb = 0; yb < w; yb += RB * R) {
+    const int y = yb + ty * R;  // first of this thread's R rows
+    const bool act = ty < RB && y < w;
+    if (act) {
+      float4 acc[R];
+#pragma unroll
+      for (int j = 0; j < R; j++) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+      const bool yin = (y >= ry && y + R - 1 + ry < w);
       const int* rt = rtab + PK_MAXR + y - ry;
-      for (int k = 0; k <= 2 * ry; k++) {
-        const float4 v = *reinterpret_cast<const float4*>(interior ? p + k * w : C + rt[k] * w + x0);
-        const float wk = wy[k];
-        acc.x = fmaf(wk, v.x, acc.x); acc.y = fmaf(wk, v.y, acc.y);
-        acc.z = fmaf(wk, v.z, acc.z); acc.w = fmaf(wk, v.w, acc.w);
+      float wr[R];
+#pragma unroll
+      for (int j = 0; j < R; j++) wr[j] = 0.0f;
+      for (int t = 0; t <= 2 * ry + R - 1; t++) {
+        // wr[j] = wy[t - j]
+#pragma unroll
+        for (int j = R - 1; j > 0; j--) wr[j] = wr[j - 1];
+        wr[0] = t <= 2 * ry ? wy[t] : 0.0f;
+        const int row = yin ? (y - ry + t) : rt[t];
+        const float4 v = *reinterpret_cast<const float4*>(C + row * w + x0);
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+          if (t - j >= 0 && t - j <= 2 * ry) {
+            const float wk = wr[j];
+            acc[j].x = fmaf(wk, v.x, acc[j].x); acc[j].y = fmaf(wk, v.y, acc[j].y);
+            acc[j].z = fmaf(wk, v.z, acc[j].z); acc[j].w = fmaf(wk, v.w, acc[j].w);
+          }
+        }
       }
-      *reinterpret_cast<float4*>(V + ty * w + x0) = acc;
+#pragma unroll
+      for (int j = 0; j < R; j++)
+        if (y + j < w) *reinterpret_cast<float4*>(V + (ty * R + j) * VP + x0) = acc[j];
     }
     __syncthreads();
-    if (y < w && ty < RB) {
-      const float* vr = V + ty * w;
-      const int x0 = tx << 2;
-      const bool interior = (x0 >= rx && x0 + 3 + rx < w);
-      const int* rt = rtab + PK_MAXR + x0 - rx;
-      const float* q = vr + x0 - rx;
-      float a0 = interior ? q[0] : vr[rt[0]];
-      float a1 = interior ? q[1] : vr[rt[1]];
-      float a2 = interior ? q[2] : vr[rt[2]];
-      float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
-      for (int k = 0; k <= 2 * rx; k++) {
-        const float a3 = interior ? q[k + 3] : vr[rt[k + 3]];
-        const float wk = wx[k];
-        f0 = fmaf(wk, a0, f0); f1 = fmaf(wk, a1, f1); f2 = fmaf(wk, a2, f2); f3 = fmaf(wk, a3, f3);
-        a0 = a1; a1 = a2; a2 = a3;
-      }
-      const float fv[4] = {f0, f1, f2, f3};
+    if (act) {
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const float f = fv[j];
-        const int x = x0 + j;
-        bool in = true;
-        if (MODE == 1) {
-          const int dy = y - mS, dx = x - mS;
-          in = !use_mask || (dy * dy + dx * dx < mS * mS);
-          const float mv = in ? f : 0.0f;
-          const int idx = y * w + x;
-          if (mv > bv || (mv == bv && idx < bi)) { bv = mv; bi = idx; }
+      for (int j = 0; j < R; j++) {
+        const int yy = y + j;
+        if (yy >= w) break;
+        const float* vr = V + (ty * R + j) * VP;
+        float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+        if (xin) {
+          const float* pp = vr + x0 - rx - OFF;
+          switch (OFF) {
+            case 0: hrow4<0>(pp, wx, rx, f0, f1, f2, f3); break;
+            case 1: hrow4<1>(pp, wx, rx, f0, f1, f2, f3); break;
+            case 2: hrow4<2>(pp, wx, rx, f0, f1, f2, f3); break;
+            default: hrow4<3>(pp, wx, rx, f0, f1, f2, f3); break;
+          }
+        } else {
+          const int* rt = rtab + PK_MAXR + x0 - rx;
+          float a0 = vr[rt[0]], a1 = vr[rt[1]], a2 = vr[rt[2]];
+          for (int k = 0; k <= 2 * rx; k++) {
+            const float a3 = vr[rt[k + 3]];
+            const float wk = wx[k];
+            f0 = fmaf(wk, a0, f0); f1 = fmaf(wk, a1, f1); f2 = fmaf(wk, a2, f2); f3 = fmaf(wk, a3, f3);
+            a0 = a1; a1 = a2; a2 = a3;
+          }
         }
-        if (in) {
-          const float d = f - c;
-          s1 += d;
-          s2 = fmaf(d, d, s2);
-          mx = fmaxf(mx, f);
-          cnt++;
+        const float fv[4] = {f0, f1, f2, f3};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const float f = fv[q];
+          const int x = x0 + q;
+          bool in = true;
+          if (MODE == 1) {
+            const int dy = yy - mS, dx = x - mS;
+            in = !use_mask || (dy * dy + dx * dx < mS * mS);
+            const float mv = in ? f : 0.0f;
+            const int idx = yy * w + x;
+            if (mv > bv || (mv == bv && idx < bi)) { bv = mv; bi = idx; }
+          }
+          if (in) {
+            const float d = f - c;
+            s1 += d;
+            s2 = fmaf(d, d, s2);
+            mx = fmaxf(mx, f);
+            cnt++;
+          }
         }
       }
     }
@@ -296,15 +373,18 @@ template <int MODE>
 __device__ void filter_any(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx, const float* wy,
                            const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st, float& amax,
                            int& aidx) {
-  if ((w & 3) == 0 && w >= 16 && w <= 4 * PK_TX)
-    filter_pass4<MODE>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
-  else
+  if ((w & 3) == 0 && w >= 16 && w <= 4 * PK_TX) {
+    if (pk_vec_rows(w) == 4)
+      filter_pass4<MODE, 4>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
+    else
+      filter_pass4<MODE, 2>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
+  } else
     filter_pass<MODE>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
 }
 
 __device__ double objective(const float* C, float* V, const int* rtab, int w, int mS, double sigma, float c,
                             PkShared& sh) {
-  const int r = gauss_weights(sigma, sh.wy);
+  const int r = gauss_weights(sigma, sh.wy, sh);
   __syncthreads();
   FiltStats st;
   float am;
@@ -445,8 +525,8 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
     sigy = p.conv_sigma_y;
     sigx = p.conv_sigma_x;
   }
-  const int ry = gauss_weights(sigy, sh.wy);
-  const int rx = gauss_weights(sigx, sh.wx);
+  const int ry = gauss_weights(sigy, sh.wy, sh);
+  const int rx = gauss_weights(sigx, sh.wx, sh);
   __syncthreads();
   FiltStats st;
   float amax = 0.0f;
@@ -496,18 +576,25 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
       }
       __syncthreads();
       // Upsampled inverse DFT on an L x L grid, L = 16*sp: frequencies -8..7.
+      // exp(+2 pi i m / L) for m in [0, L) is staged in shared memory after
+      // the L x 16 intermediate.
       const int L = 16 * sp;
       const int tws = TWN / L;
       float2* Tx = (float2*)C;  // the window is no longer needed
+      float2* Wl = Tx + 16 * L;
+      __syncthreads();
+      for (int m = threadIdx.x; m < L; m += PK_T) {
+        float2 t = __ldg(tw + m * tws);
+        t.y = -t.y;
+        Wl[m] = t;
+      }
       __syncthreads();
       for (int e = threadIdx.x; e < 16 * L; e += PK_T) {
         const int fyi = e / L, nx = e - fyi * L;
         float2 acc = make_float2(0.0f, 0.0f);
         for (int fxi = 0; fxi < 16; fxi++) {
           const int fx = fxi - 8;
-          const int m = ((fx * nx) % L + L) % L;
-          float2 t = __ldg(tw + m * tws);
-          t.y = -t.y;  // exp(+2 pi i m / L)
+          const float2 t = Wl[(fx * nx) & (L - 1)];
           acc = cadd(acc, cmul(patchF[((fyi - 8) & 15) * 16 + (fx & 15)], t));
         }
         Tx[fyi * L + nx] = acc;
@@ -521,9 +608,7 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
         float2 acc = make_float2(0.0f, 0.0f);
         for (int fyi = 0; fyi < 16; fyi++) {
           const int fy = fyi - 8;
-          const int m = ((fy * ny) % L + L) % L;
-          float2 t = __ldg(tw + m * tws);
-          t.y = -t.y;
+          const float2 t = Wl[(fy * ny) & (L - 1)];
           acc = cadd(acc, cmul(Tx[fyi * L + nx], t));
         }
         const float mag = sqrtf(acc.x * acc.x + acc.y * acc.y) * invL2;
@@ -574,11 +659,13 @@ extern "C" int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr
     return set_error(ZR_ESIZE, "zr_locate_peaks: opti sigma bound too large");
   const float2* tw = twiddles();
   if (!tw) return ZR_ECUDA;
-  // window + one block of filtered rows (at most PK_T*4 floats for the
-  // vectorised layout, PK_RB rows otherwise)
-  const size_t vbuf = (size_t)((4 * PK_T > PK_RB * w) ? 4 * PK_T : PK_RB * w) * sizeof(float);
+  // window + one block of filtered rows (RB lanes x pk_vec_rows rows at pitch
+  // w + 8 for the vectorised layout, PK_RB rows otherwise)
+  const bool vec = (w & 3) == 0 && w >= 16 && w <= 4 * PK_TX;
+  const size_t vrows = vec ? (size_t)(PK_T / (w / 4)) * pk_vec_rows(w) : (size_t)PK_RB;
+  const size_t vbuf = vrows * (vec ? pk_vec_pitch(w) : w) * sizeof(float);
   size_t smem = (size_t)w * w * sizeof(float) + vbuf;
-  const size_t sub = (size_t)16 * 16 * params->sub_pix_reg * sizeof(float2);
+  const size_t sub = (size_t)17 * 16 * params->sub_pix_reg * sizeof(float2);
   if (params->sub_pix_reg > 1 && (size_t)w * w * sizeof(float) < sub) smem = sub + vbuf;
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_peaks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_peaks attr"));

@@ -23,7 +23,14 @@
 
 namespace zr {
 
+#ifndef ZR_XC_EPT
+#define ZR_XC_EPT 32
+#endif
 constexpr int XC_NBC = 4;  // columns per CTA in the column pass
+// elements per thread of the column-pass transforms (two radix-16 butterflies
+// per thread and pass): 256 threads of <= 128 registers for a 2048-point
+// crop, two CTAs per SM; measured faster than one butterfly per thread
+constexpr int XC_EPT = ZR_XC_EPT;
 constexpr int XC_NBR = 2;  // packed row pairs per CTA in the row pass
 
 struct XcJobs {
@@ -55,9 +62,9 @@ __device__ __forceinline__ void job_operands(const XcJobs& J, int job, const flo
 }
 
 template <int C0>
-__global__ void __launch_bounds__(fft_threads(C0, XC_NBC), fft_minblocks(C0))
+__global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks(C0))
     k_xc_cols(XcJobs J, int C1, int K4, int mS, float2* __restrict__ Tw, const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(C0, XC_NBC);
+  constexpr int T = fft_threads(C0, XC_NBC, XC_EPT);
   constexpr int LD = ld_of(C0);
   extern __shared__ float2 sm[];
   // jobs vary fastest across the grid so that the CTAs resident at one time
@@ -182,7 +189,7 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
 template <int C0>
 static int launch_xc_cols(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
                           cudaStream_t st) {
-  constexpr int T = fft_threads(C0, XC_NBC);
+  constexpr int T = fft_threads(C0, XC_NBC, XC_EPT);
   const size_t smem = (size_t)XC_NBC * ld_of(C0) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_xc_cols attr"));

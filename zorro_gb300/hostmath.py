@@ -92,121 +92,20 @@ def l1_solve(A, b, w, lo, hi):
     return res.x[:n]
 
 
-def _logistic_cdf_error(x, hSigma, cdf):
-    """The logistic-CDF error of zorro_util.py:862-863 (float64).  Callers
-    silence the overflow warning of exp (np.errstate) around the whole fit."""
-    model = 1.0 - 1.0 / (1.0 + np.exp(-x[1] * (-hSigma + x[0]))) ** x[2]
-    return np.sum(np.abs(cdf - model))
-
-
-def _logistic_objective(hSigma, cdf):
-    """_logistic_cdf_error(x, hSigma, cdf) as a closure with -hSigma computed
-    once; every element goes through the same operations, so the values are
-    the same."""
-    nh = -hSigma
-    exp, absolute = np.exp, np.abs
-
-    def f(x):
-        return absolute(cdf - (1.0 - 1.0 / (1.0 + exp(-x[1] * (nh + x[0]))) ** x[2])).sum()
-    return f
-
-
-def nelder_mead_bounded(f, x0, lo, hi, xatol, fatol, maxiter, maxfev):
-    """Bounded Nelder-Mead, step for step the method of
-    scipy.optimize.minimize(method='Nelder-Mead', bounds=...) with its
-    default (non-adaptive) coefficients: the same start simplex (5 % steps,
-    reflected into the box), reflection, expansion, outside and inside
-    contraction, shrink, clipping to the box and stopping tests, so that it
-    returns the same point.  The simplex lives in Python floats instead of
-    small arrays, which removes most of the per-iteration overhead; ``f`` is
-    called with a float64 array as scipy calls it."""
-    n = len(x0)
-    x0 = [min(max(float(v), lo[k]), hi[k]) for k, v in enumerate(x0)]
-    sim = [list(x0)]
-    for k in range(n):
-        y = list(x0)
-        y[k] = (1 + 0.05) * y[k] if y[k] != 0 else 0.00025
-        sim.append(y)
-    sim = [[min(max(2 * hi[k] - v if v > hi[k] else v, lo[k]), hi[k]) for k, v in enumerate(p)] for p in sim]
-    calls = [0]
-
-    class _MaxFev(Exception):
-        pass
-
-    def fx(p):
-        if calls[0] >= maxfev:
-            raise _MaxFev()
-        calls[0] += 1
-        return float(f(np.array(p, dtype=np.float64)))
-
-    def clip(p):
-        return [min(max(v, lo[k]), hi[k]) for k, v in enumerate(p)]
-
-    def order(sim, fs):
-        # np.argsort as scipy sorts (its tie order included)
-        idx = np.argsort(np.array(fs)).tolist()
-        return [sim[i] for i in idx], [fs[i] for i in idx]
-
-    fs = [np.inf] * (n + 1)
-    try:
-        for k in range(n + 1):
-            fs[k] = fx(sim[k])
-    except _MaxFev:
-        pass
-    sim, fs = order(sim, fs)
-    it = 1
-    while calls[0] < maxfev and it < maxiter:
-        try:
-            if (max(abs(sim[i][k] - sim[0][k]) for i in range(1, n + 1) for k in range(n)) <= xatol and
-                    max(abs(fs[0] - fs[i]) for i in range(1, n + 1)) <= fatol):
-                break
-            xbar = [v / n for v in [sum_rows(sim, k, n) for k in range(n)]]
-            last = sim[-1]
-            xr = clip([2 * xbar[k] - last[k] for k in range(n)])
-            fxr = fx(xr)
-            shrink = False
-            if fxr < fs[0]:
-                xe = clip([3 * xbar[k] - 2 * last[k] for k in range(n)])
-                fxe = fx(xe)
-                if fxe < fxr:
-                    sim[-1], fs[-1] = xe, fxe
-                else:
-                    sim[-1], fs[-1] = xr, fxr
-            elif fxr < fs[-2]:
-                sim[-1], fs[-1] = xr, fxr
-            else:
-                if fxr < fs[-1]:
-                    xc = clip([1.5 * xbar[k] - 0.5 * last[k] for k in range(n)])
-                    fxc = fx(xc)
-                    if fxc <= fxr:
-                        sim[-1], fs[-1] = xc, fxc
-                    else:
-                        shrink = True
-                else:
-                    xcc = clip([0.5 * xbar[k] + 0.5 * last[k] for k in range(n)])
-                    fxcc = fx(xcc)
-                    if fxcc < fs[-1]:
-                        sim[-1], fs[-1] = xcc, fxcc
-                    else:
-                        shrink = True
-                if shrink:
-                    for j in range(1, n + 1):
-                        sim[j] = clip([sim[0][k] + 0.5 * (sim[j][k] - sim[0][k]) for k in range(n)])
-                        fs[j] = fx(sim[j])
-            it += 1
-        except _MaxFev:
-            pass
-        sim, fs = order(sim, fs)
-    return np.array(sim[0]), min(fs), calls[0]
-
-
-def sum_rows(sim, k, n):
-    """sim[0][k] + sim[1][k] + ... + sim[n-1][k] in row order (the centroid
-    numerator, as np.add.reduce(sim[:-1], 0) forms it)."""
-    acc = sim[0][k]
-    for i in range(1, n):
-        acc = acc + sim[i][k]
-    return acc
+def logistic_nelder_mead(hSigma, cdf, x0, lo, hi, xatol=1e-10, fatol=1e-14, maxiter=4000, maxfev=8000):
+    """Bounded Nelder-Mead on the logistic-CDF error (zr_logistic_fit, host
+    C++): the steps of scipy.optimize.minimize(method='Nelder-Mead',
+    bounds=...), so it returns scipy's point wherever NumPy's exp and pow are
+    the C library's (as on aarch64)."""
+    import ctypes as C
+    from . import _lib
+    h = np.ascontiguousarray(hSigma, dtype=np.float64)
+    c = np.ascontiguousarray(cdf, dtype=np.float32)
+    a0, alo, ahi = (np.ascontiguousarray(v, dtype=np.float64) for v in (x0, lo, hi))
+    x = np.zeros(3)
+    _lib.call("zr_logistic_fit", h.ctypes.data, c.ctypes.data, len(h), a0.ctypes.data, alo.ctypes.data,
+              ahi.ctypes.data, float(xatol), float(fatol), int(maxiter), int(maxfev), x.ctypes.data, None, None)
+    return x
 
 
 def logistic_fit(peaksigTriMat):
@@ -226,11 +125,7 @@ def logistic_fit(peaksigTriMat):
     pdf = pdf.astype("float32")
     cdf = np.cumsum(pdf)
     cdf /= cdf[-1]
-    lo = (float(np.min(ps)), 0.1, 0.05)
-    hi = (float(np.max(ps)), 20.0, 5.0)
-    with np.errstate(over="ignore"):
-        x, _, _ = nelder_mead_bounded(_logistic_objective(hSigma, cdf), (np.mean(ps), 5.0, 1.0), lo, hi,
-                                      xatol=1e-10, fatol=1e-14, maxiter=4000, maxfev=8000)
+    x = logistic_nelder_mead(hSigma, cdf, (np.mean(ps), 5.0, 1.0), (np.min(ps), 0.1, 0.05), (np.max(ps), 20.0, 5.0))
     return {"peaksigThres": x[0], "logisticK": x[1], "logisticNu": x[2], "pdfPeaks": pdf, "cdfPeaks": cdf,
             "hSigma": hSigma}
 
