@@ -165,6 +165,9 @@ int zr_spectra(const zr_frames_t* frames, const float* mask, const double* mean_
 
 /* ---- masked normalised cross-correlation: mnxc2, zorro.py:1014-1097 ---- */
 
+/* Scratch of the correlation passes: (2*max_shift + 1) rows of
+ * zr_spectrum_pitch(C1) complex values per job of a wave; any size from one
+ * job up works (larger means fewer, bigger waves). */
 size_t zr_xcorr_work_bytes(int n_jobs, int C1, int max_shift);
 
 /* The frame-only terms of mnxc2, windowed: for every frame n the windows of

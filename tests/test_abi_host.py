@@ -40,7 +40,7 @@ def test_size_queries(lib):
     assert lib.zr_version() >= 100
     assert lib.zr_spectrum_pitch(2048) == 1028
     assert lib.zr_spectrum_elems(2048, 2048) == 2052 * 1028
-    assert lib.zr_xcorr_work_bytes(10, 2048, 100) == 10 * 200 * 1028 * 8
+    assert lib.zr_xcorr_work_bytes(10, 2048, 100) == 10 * 201 * 1028 * 8
 
 
 def test_errors_are_reported_without_a_gpu(lib):

@@ -17,7 +17,10 @@
 // The four frame-only terms (CorrTM, CorrBM and the two Denominator IFFTs)
 // depend on one frame each, so they are computed once per frame (zr_xcorr_terms)
 // instead of once per pair; the pair kernel only transforms the numerator
-// G_J conj(G_I) and combines.
+// G_J conj(G_I) and combines.  Since real(IFFT(A conj(B)))(y, x) =
+// real(IFFT(conj(A) B))(-y, -x) for any spectra, CorrTM is CorrBM and DenomT
+// is DenomB point-reflected: one transform per frame gives both, over the
+// (w+1) x (w+1) window [-maxShift, maxShift]^2 that the reflection needs.
 #include "common.cuh"
 #include "internal.h"
 
@@ -42,6 +45,7 @@ struct XcJobs {
   int kind;          // 0 terms, 1 pairs
   int job0;
   long long se;      // spectrum elements
+  int rows;          // window rows kept by the column pass: w + 1 (terms) or w (pairs)
 };
 
 __device__ __forceinline__ void job_operands(const XcJobs& J, int job, const float2*& A, const float2*& B) {
@@ -53,10 +57,8 @@ __device__ __forceinline__ void job_operands(const XcJobs& J, int job, const flo
   }
   const int t = job / J.N, n = job - t * J.N;
   switch (t) {
-    case 0: A = J.GM; B = J.G + (size_t)n * J.se; break;   // CorrTM: M * conj(G_I)
-    case 1: A = J.G + (size_t)n * J.se; B = J.GM; break;   // CorrBM: conj(M) * G_J
-    case 2: A = J.GM; B = J.S + (size_t)n * J.se; break;   // DenomT: M * conj(S_I)
-    case 3: A = J.S + (size_t)n * J.se; B = J.GM; break;   // DenomB: conj(M) * S_J
+    case 0: A = J.G + (size_t)n * J.se; B = J.GM; break;   // CorrBM: conj(M) * G_n (and CorrTM)
+    case 1: A = J.S + (size_t)n * J.se; B = J.GM; break;   // DenomB: conj(M) * S_n (and DenomT)
     default: A = J.GM; B = J.GM; break;                     // maskProduct
   }
 }
@@ -122,9 +124,9 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks
   }
   __syncthreads();
   block_fft<C0, XC_NBC, T, 1>(sm, tw);
-  const int w = 2 * mS;
-  float2* out = Tw + (size_t)jl * w * K4;
-  for (int e = threadIdx.x; e < w * XC_NBC; e += T) {
+  const int rows = J.rows;
+  float2* out = Tw + (size_t)jl * rows * K4;
+  for (int e = threadIdx.x; e < rows * XC_NBC; e += T) {
     const int a = e / XC_NBC, c = e - a * XC_NBC;
     const int y = (a - mS) & (C0 - 1);
     out[(size_t)a * K4 + k0 + c] = sm[c * LD + pidx(y)];
@@ -140,15 +142,16 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
   constexpr int half = C1 / 2;
   extern __shared__ float2 sm[];
   const int w = 2 * mS;
+  const int rows = J.rows;  // w + 1 for the frame terms (rows and columns -mS..mS)
   const int jl = blockIdx.y;
   const int job = J.job0 + jl;
   const int arow0 = blockIdx.x * (2 * XC_NBR);
-  const float2* src = Tw + (size_t)jl * w * K4;
+  const float2* src = Tw + (size_t)jl * rows * K4;
   for (int e = threadIdx.x; e < XC_NBR * (half + 1); e += T) {
     const int p = e / (half + 1), k = e - p * (half + 1);
     const int a0 = arow0 + 2 * p, a1 = a0 + 1;
-    const float2 ga = a0 < w ? src[(size_t)a0 * K4 + k] : make_float2(0.0f, 0.0f);
-    const float2 gb = a1 < w ? src[(size_t)a1 * K4 + k] : make_float2(0.0f, 0.0f);
+    const float2 ga = a0 < rows ? src[(size_t)a0 * K4 + k] : make_float2(0.0f, 0.0f);
+    const float2 gb = a1 < rows ? src[(size_t)a1 * K4 + k] : make_float2(0.0f, 0.0f);
     float2* s = sm + p * LD;
     if (k == 0 || k == half) {
       s[pidx(k)] = make_float2(ga.x, gb.x);
@@ -160,17 +163,25 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
   __syncthreads();
   block_fft<C1, XC_NBR, T, 1>(sm, tw);
   const size_t w2 = (size_t)w * w;
-  for (int e = threadIdx.x; e < XC_NBR * 2 * w; e += T) {
-    const int q = e / w, b = e - q * w;
+  const int cols = rows;  // the terms window is square, w + 1 wide
+  for (int e = threadIdx.x; e < XC_NBR * 2 * cols; e += T) {
+    const int q = e / cols, b = e - q * cols;
     const int p = q >> 1;
     const int a = arow0 + q;
-    if (a >= w) continue;
+    if (a >= rows) continue;
     const int x = (b - mS) & (C1 - 1);
     const float2 yv = sm[p * LD + pidx(x)];
     const float v = ((q & 1) ? yv.y : yv.x) * scale;
     const size_t pix = (size_t)a * w + b;
     if (J.kind == 0) {
-      out[(size_t)job * w2 + pix] = v;
+      // output slots: CorrTM [0,N), CorrBM [N,2N), DenomT [2N,3N), DenomB [3N,4N), maskProduct 4N
+      const int t = job / J.N, n = job - t * J.N;
+      const int main_slot = t == 0 ? J.N + n : (t == 1 ? 3 * J.N + n : 4 * J.N);
+      if (a < w && b < w) out[(size_t)main_slot * w2 + pix] = v;
+      if (t < 2 && a >= 1 && b >= 1) {
+        const int refl_slot = t == 0 ? n : 2 * J.N + n;
+        out[(size_t)refl_slot * w2 + (size_t)(w - a) * w + (w - b)] = v;
+      }
     } else {
       const int I = J.pairs[2 * job], Jj = J.pairs[2 * job + 1];
       const int N = J.N;
@@ -204,9 +215,8 @@ static int launch_xc_rows(const XcJobs& J, int nj, int C0, int K4, int mS, float
   const size_t smem = (size_t)XC_NBR * ld_of(C1) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_rows<C1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_xc_rows attr"));
-  const int w = 2 * mS;
-  k_xc_rows<C1><<<dim3((w + 2 * XC_NBR - 1) / (2 * XC_NBR), nj), T, smem, st>>>(J, C0, K4, mS, scale, Tw, terms,
-                                                                               out, tw);
+  k_xc_rows<C1><<<dim3((J.rows + 2 * XC_NBR - 1) / (2 * XC_NBR), nj), T, smem, st>>>(J, C0, K4, mS, scale, Tw,
+                                                                                    terms, out, tw);
   return launched("k_xc_rows");
 }
 
@@ -225,8 +235,7 @@ static int launch_xc_rows(const XcJobs& J, int nj, int C0, int K4, int mS, float
 static int run_jobs(XcJobs J, int njobs, int C0, int C1, int mS, const float* terms, float* out, void* work,
                     size_t work_bytes, cudaStream_t st) {
   const int K4 = zr_spectrum_pitch(C1);
-  const int w = 2 * mS;
-  const size_t per_job = (size_t)w * K4 * sizeof(float2);
+  const size_t per_job = (size_t)J.rows * K4 * sizeof(float2);
   if (!work || work_bytes < per_job)
     return set_error(ZR_EWORK, "zr_xcorr: work buffer %zu bytes < %zu (one job)", work_bytes, per_job);
   const int wave = (int)((work_bytes / per_job) < (size_t)njobs ? work_bytes / per_job : (size_t)njobs);
@@ -257,15 +266,16 @@ static int check_sizes(int C0, int C1, int mS) {
 using namespace zr;
 
 extern "C" size_t zr_xcorr_work_bytes(int n_jobs, int C1, int max_shift) {
-  return (size_t)n_jobs * 2 * max_shift * zr_spectrum_pitch(C1) * sizeof(float2);
+  return (size_t)n_jobs * (2 * max_shift + 1) * zr_spectrum_pitch(C1) * sizeof(float2);
 }
 
 extern "C" int zr_xcorr_terms(const void* G, const void* S, const void* GM, int N, int C0, int C1, int max_shift,
                               float* terms, void* work, size_t work_bytes, void* stream) {
   if (!G || !S || !GM || !terms || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_terms: null argument");
   ZR_TRY(check_sizes(C0, C1, max_shift));
-  XcJobs J{(const float2*)G, (const float2*)S, (const float2*)GM, nullptr, N, 0, 0, zr_spectrum_elems(C0, C1)};
-  return run_jobs(J, 4 * N + 1, C0, C1, max_shift, nullptr, terms, work, work_bytes, (cudaStream_t)stream);
+  XcJobs J{(const float2*)G, (const float2*)S, (const float2*)GM, nullptr, N, 0, 0, zr_spectrum_elems(C0, C1),
+           2 * max_shift + 1};
+  return run_jobs(J, 2 * N + 1, C0, C1, max_shift, nullptr, terms, work, work_bytes, (cudaStream_t)stream);
 }
 
 extern "C" int zr_xcorr_pairs(const void* G, const float* terms, const int* pairs, int M, int N, int C0, int C1,
@@ -273,6 +283,6 @@ extern "C" int zr_xcorr_pairs(const void* G, const float* terms, const int* pair
   if (!G || !terms || !pairs || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_pairs: null argument");
   if (M <= 0) return ZR_OK;
   ZR_TRY(check_sizes(C0, C1, max_shift));
-  XcJobs J{(const float2*)G, nullptr, nullptr, pairs, N, 1, 0, zr_spectrum_elems(C0, C1)};
+  XcJobs J{(const float2*)G, nullptr, nullptr, pairs, N, 1, 0, zr_spectrum_elems(C0, C1), 2 * max_shift};
   return run_jobs(J, M, C0, C1, max_shift, terms, cwin, work, work_bytes, (cudaStream_t)stream);
 }
