@@ -173,3 +173,24 @@ def test_logistic_fit_converges_to_a_minimum():
                                         options={"xatol": 1e-10, "fatol": 1e-14, "maxiter": 4000, "maxfev": 8000})
             fx = zo._logistic_cdf_error64(x, h, cdf)
         assert fx <= r.fun * (1 + 1e-6) + 1e-9, (trial, fx, r.fun)
+
+
+def test_hotpix_fit_bit_exact_over_random_histograms():
+    """The product's CDF fit (L-BFGS-B with the forward-difference gradient
+    passed in) returns the oracle's scipy L-BFGS-B result bit for bit."""
+    rng = np.random.default_rng(3)
+    info = dict(zo.DEFAULTS["hotpixInfo"])
+    for t in range(12):
+        usum = rng.poisson(rng.uniform(5, 60), (200, 150)).astype(np.float32)
+        if t % 3 == 0:
+            usum[rng.random(usum.shape) < 1e-3] *= 20
+        if t % 4 == 0:
+            usum[rng.random(usum.shape) < 1e-3] = 0
+        mean = float(np.sum(usum, dtype=np.float64)) / usum.size
+        sm, ps, edges = hm.hotpix_bins(mean, info["maxSigma"])
+        hist, _ = np.histogram(usum, edges)
+        mu, sg, cl, cu, _ = hm.hotpix_fit(hist, edges, sm, ps, dict(info))
+        ref = zo.hotpix_fit(usum, dict(info), 20, zo.Dtypes(True))
+        assert mu == ref["mu"] and sg == ref["sigma"], t
+        assert cu == ref["cutoffUpper"], t
+        assert cl == ref["cutoffLower"] or (np.isnan(cl) and np.isnan(ref["cutoffLower"])), t

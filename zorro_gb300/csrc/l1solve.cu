@@ -123,6 +123,22 @@ extern "C" int zr_l1_solve(const double* A, const double* b, const double* w, in
       out[j - m] = sgn[j - m];
     }
   };
+  // Pricing state of every variable: act[j] = 1 for a nonbasic variable that
+  // can move (0 for basic or fixed ones), up[j] = +1 at its upper bound, -1 at
+  // its lower bound; the gain of moving it is up[j] * d_j (d_j its reduced
+  // cost), so the pricing loop has no data-dependent branches.
+  std::vector<double> act(NV), up(NV), rc(NV);
+  auto set_state = [&](int j) {
+    act[j] = (where[j] < 0 && ub[j] - lb[j] > 0.0) ? 1.0 : 0.0;
+    up[j] = val[j] <= lb[j] ? -1.0 : 1.0;
+  };
+  auto compute_pi = [&]() {  // duals pi = c_B^T B^-1
+    for (int k = 0; k < n; k++) {
+      double s = 0.0;
+      for (int i = 0; i < n; i++) s += cost[basis[i]] * Binv[(size_t)i * n + k];
+      pi[k] = s;
+    }
+  };
   int iters = 0;
   const int max_iters = 50 * (m + n) + 1000;
   for (int phase = 1; phase <= 2; phase++) {
@@ -131,47 +147,48 @@ extern "C" int zr_l1_solve(const double* A, const double* b, const double* w, in
       // artificials are fixed at zero from here on
       for (int i = 0; i < n; i++) ub[m + i] = 0.0;
     }
-    int degenerate_run = 0;
+    for (int j = 0; j < NV; j++) set_state(j);
+    compute_pi();
+    int degenerate_run = 0, since_refresh = 0;
     for (;;) {
       if (++iters > max_iters) {
         if (status) *status = 2;
         return set_error(ZR_EINVAL, "zr_l1_solve: iteration limit");
       }
-      // duals pi = c_B^T B^-1
-      for (int k = 0; k < n; k++) {
-        double s = 0.0;
-        for (int i = 0; i < n; i++) s += cost[basis[i]] * Binv[(size_t)i * n + k];
-        pi[k] = s;
+      if (++since_refresh >= 32) {  // bound the drift of the updated duals
+        compute_pi();
+        since_refresh = 0;
       }
+      // reduced costs
       if (runs) {
         pre[0] = 0.0;
         for (int k = 0; k < n; k++) pre[k + 1] = pre[k] + pi[k];
-      }
-      // entering variable
-      const bool bland = degenerate_run > 50;
-      int enter = -1;
-      double best = 0.0, dir = 0.0;
-      for (int j = 0; j < NV; j++) {
-        if (where[j] >= 0 || ub[j] - lb[j] <= 0.0) continue;
-        double d = cost[j];
-        if (j < m && runs) {
-          if (r0[j] >= 0) d -= pre[r1[j]] - pre[r0[j]];
-        } else if (j < m) {
+        for (int j = 0; j < m; j++) rc[j] = cost[j] - (r0[j] >= 0 ? pre[r1[j]] - pre[r0[j]] : 0.0);
+      } else {
+        for (int j = 0; j < m; j++) {
+          double d = cost[j];
           const double* aj = A + (size_t)j * n;
           for (int i = 0; i < n; i++) d -= pi[i] * aj[i];
-        } else {
-          d -= pi[j - m] * sgn[j - m];
+          rc[j] = d;
         }
-        const bool at_lo = val[j] <= lb[j];
-        double gain = 0.0, dj = 0.0;
-        if (at_lo && d < -tol) { gain = -d; dj = 1.0; }
-        else if (!at_lo && d > tol) { gain = d; dj = -1.0; }
-        if (gain > 0.0) {
-          if (bland) { enter = j; dir = dj; break; }
-          if (gain > best) { best = gain; enter = j; dir = dj; }
+      }
+      for (int i = 0; i < n; i++) rc[m + i] = cost[m + i] - pi[i] * sgn[i];
+      // entering variable: largest gain (Dantzig), or the first improving
+      // variable (Bland) after a run of degenerate pivots
+      const bool bland = degenerate_run > 50;
+      int enter = -1;
+      double best = tol;
+      for (int j = 0; j < NV; j++) {
+        const double gain = act[j] * up[j] * rc[j];
+        if (gain > best) {
+          enter = j;
+          if (bland) break;
+          best = gain;
         }
       }
       if (enter < 0) break;  // optimal for this phase
+      const double dir = -up[enter];
+      const double d_enter = rc[enter];
       if (runs && enter < m) {
         for (int i = 0; i < n; i++) {
           double s = 0.0;
@@ -215,6 +232,7 @@ extern "C" int zr_l1_solve(const double* A, const double* b, const double* w, in
       val[enter] += dir * tmax;
       if (leave < 0) {
         val[enter] = dir > 0 ? ub[enter] : lb[enter];  // bound flip
+        set_state(enter);
         continue;
       }
       const int out = basis[leave];
@@ -222,6 +240,8 @@ extern "C" int zr_l1_solve(const double* A, const double* b, const double* w, in
       where[out] = -1;
       basis[leave] = enter;
       where[enter] = leave;
+      set_state(out);
+      set_state(enter);
       // B^-1 update with pivot alpha[leave]
       const double piv = alpha[leave];
       for (int k = 0; k < n; k++) Binv[(size_t)leave * n + k] /= piv;
@@ -230,6 +250,8 @@ extern "C" int zr_l1_solve(const double* A, const double* b, const double* w, in
         const double f = alpha[i];
         for (int k = 0; k < n; k++) Binv[(size_t)i * n + k] -= f * Binv[(size_t)leave * n + k];
       }
+      // duals after the pivot: pi += d_enter * (new row `leave` of B^-1)
+      for (int k = 0; k < n; k++) pi[k] += d_enter * Binv[(size_t)leave * n + k];
     }
     if (phase == 1) {
       double infeas = 0.0;

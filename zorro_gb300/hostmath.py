@@ -282,6 +282,40 @@ def hotpix_bins(sumMean, maxSigma):
     return sumMean, poissonStd, edges
 
 
+def _forward_difference(f, bounds, step=1e-8):
+    """The gradient L-BFGS-B estimates when no jac is given (scipy's 2-point
+    approx_derivative with absolute step ``step``, the steps turned around or
+    shortened to stay inside ``bounds``), as a jac callable: the same
+    numbers without the general machinery's per-call overhead."""
+    lb = np.array([b[0] for b in bounds], dtype=np.float64)
+    ub = np.array([b[1] for b in bounds], dtype=np.float64)
+    eps2 = np.finfo(np.float64).eps ** 0.5
+
+    def grad(x):
+        x0 = np.asarray(x, dtype=np.float64)
+        f0 = f(x0)
+        sign_x0 = (x0 >= 0).astype(np.float64) * 2 - 1
+        h = np.full(x0.shape, step)
+        dx = (x0 + h) - x0
+        h = np.where(dx == 0, eps2 * sign_x0 * np.maximum(1.0, np.abs(x0)), h)
+        lower_dist, upper_dist = x0 - lb, ub - x0
+        xs = x0 + h
+        violated = (xs < lb) | (xs > ub)
+        fitting = np.abs(h) <= np.maximum(lower_dist, upper_dist)
+        h[violated & fitting] *= -1
+        forward = (upper_dist >= lower_dist) & ~fitting
+        h[forward] = upper_dist[forward]
+        backward = (upper_dist < lower_dist) & ~fitting
+        h[backward] = -lower_dist[backward]
+        g = np.empty_like(x0)
+        for i in range(x0.size):
+            x1 = x0.copy()
+            x1[i] = x0[i] + h[i]
+            g[i] = (f(x1) - f0) / ((x0[i] + h[i]) - x0[i])
+        return g
+    return grad
+
+
 def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
     """Normal-CDF fit and the outlier cut-offs.  zorro.py:2535-2592.  An empty
     line fit falls back to the configured default, as it did when
@@ -298,9 +332,9 @@ def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
         # values without the distribution machinery's overhead
         return np.sum(np.abs(cdf - scipy.special.ndtr((counts - params[0]) / params[1])))
 
-    best = scipy.optimize.minimize(err, (sumMean, poissonStd), method="L-BFGS-B",
-                                   bounds=((sumMean - 0.5 * poissonStd, sumMean + 0.5 * poissonStd),
-                                           (0.7 * poissonStd, 1.3 * poissonStd)))
+    bounds = ((sumMean - 0.5 * poissonStd, sumMean + 0.5 * poissonStd), (0.7 * poissonStd, 1.3 * poissonStd))
+    best = scipy.optimize.minimize(err, (sumMean, poissonStd), method="L-BFGS-B", bounds=bounds,
+                                   jac=_forward_difference(err, bounds))
     with np.errstate(all="ignore"):
         sig_cdf = np.sqrt(2) * scipy.special.erfinv(2.0 * cdf - 1)
     normal = (counts - best.x[0]) / best.x[1]
