@@ -4,7 +4,8 @@
 // Each box x box tile of the even and odd sums is Hann-windowed; both real
 // tiles go through one complex FFT per row (z = e + i o), the column pass
 // transforms E and O and accumulates, per frequency and over all tiles, the
-// normalised correlation real(E conj O) / sqrt(|O|^2 |E|^2) in double.  The
+// normalised correlation real(E conj O) / sqrt(|O|^2 |E|^2) (float per tile
+// and per group of FRC_TPG tiles, the groups summed in double).  The
 // reference scales both spectra by 1/box^4 first; the ratio does not depend
 // on that scale, so it is left out (it only risks float underflow).  Only
 // kx in [0, box/2] is computed: the ratio at (-ky, -kx) equals the one at
@@ -61,8 +62,11 @@ __global__ void __launch_bounds__(fft_threads(B, FRC_NB), fft_minblocks(B))
   }
 }
 
+// CTAs per SM that keep a T-thread CTA at <= 128 registers per thread
+constexpr int frc_minblocks(int T) { return T >= 512 ? 1 : 512 / T; }
+
 template <int B>
-__global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB), fft_minblocks(B))
+__global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB), frc_minblocks(fft_threads(B, 2 * FRC_NB)))
     k_frc_cols(const float2* __restrict__ RE, const float2* __restrict__ RO, int n_tiles, int K4,
                double* __restrict__ half, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(B, 2 * FRC_NB);
@@ -72,9 +76,9 @@ __global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB), fft_minblocks(B))
   const int k0 = blockIdx.x * FRC_NB;
   const int t0 = blockIdx.y * FRC_TPG;
   const int t1 = min(n_tiles, t0 + FRC_TPG);
-  double acc[PER];
+  float acc[PER];  // at most FRC_TPG tiles per CTA; the groups are summed in double
 #pragma unroll
-  for (int i = 0; i < PER; i++) acc[i] = 0.0;
+  for (int i = 0; i < PER; i++) acc[i] = 0.0f;
   for (int t = t0; t < t1; t++) {
     const size_t tb = (size_t)t * (B / FRC_NB) * K4 * FRC_NB;
     for (int e = threadIdx.x; e < B * FRC_NB; e += T) {
@@ -92,9 +96,12 @@ __global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB), fft_minblocks(B))
       const int e = threadIdx.x + i * T;
       if (e < B * FRC_NB) {
         const int c = e / B, y = e - c * B;
+        // the tile's correlation at this frequency in float (|r| <= 1, the
+        // magnitudes taken separately so that their product cannot
+        // overflow), the sum over tiles in double
         const float2 E = sm[c * LD + pidx(y)], O = sm[(FRC_NB + c) * LD + pidx(y)];
-        const double num = (double)E.x * O.x + (double)E.y * O.y;
-        const double den = sqrt(((double)O.x * O.x + (double)O.y * O.y) * ((double)E.x * E.x + (double)E.y * E.y));
+        const float num = fmaf(E.x, O.x, E.y * O.y);
+        const float den = sqrtf(fmaf(O.x, O.x, O.y * O.y)) * sqrtf(fmaf(E.x, E.x, E.y * E.y));
         acc[i] += num / den;
       }
     }
@@ -105,7 +112,7 @@ __global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB), fft_minblocks(B))
     const int e = threadIdx.x + i * T;
     if (e < B * FRC_NB) {
       const int c = e / B, y = e - c * B;
-      half[((size_t)blockIdx.y * B + y) * K4 + k0 + c] = acc[i];
+      half[((size_t)blockIdx.y * B + y) * K4 + k0 + c] = (double)acc[i];
     }
   }
 }
