@@ -68,6 +68,12 @@ _COMPAT_EDITS = [
     (2587, "np.linalg.lstsq(", "_lstsq_strict("),
     (2413, "dosePerFrame = self.doseFiltParam[0]",
      "dosePerFrame = self.doseFiltParam[0]; missingDose = dosePerFrame * np.float32( self.doseFiltParam[5] )"),
+    # evenOddFouRingCorr's sub-registrators load the parent's config, including
+    # doEvenOddFRC=True, and recurse until a half-set has too few frames for
+    # cdfLogisticCurve (zorro.py:2128-2186): one level only
+    (2128, "evenReg.loadConfig( tempLogName )", "evenReg.loadConfig( tempLogName ); evenReg.doEvenOddFRC = False"),
+    (2132, "oddReg.loadConfig( tempLogName )", "oddReg.loadConfig( tempLogName ); oddReg.doEvenOddFRC = False"),
+    (2186, "eoReg.loadConfig( tempLogName )", "eoReg.loadConfig( tempLogName ); eoReg.doEvenOddFRC = False"),
 ]
 
 _NE_FUNCS = {
@@ -261,6 +267,11 @@ def run_reference(images, *, fp64=True, capture=False, **attrs):
         reg.cachePath = td
         for k, v in attrs.items():
             setattr(reg, k, v)
+        # evenOddFouRingCorr writes a temporary .zor into the working directory
+        # and names its half-set sums after files['sum'] (zorro.py:2121-2215)
+        reg.files = dict(reg.files)
+        if not reg.files.get("sum"):
+            reg.files["sum"] = os.path.join(td, "sum.mrc")
         cap = {"C": {}, "Cfilt": {}, "sigma": {}}
         if capture:
             orig_locate = zmod.ImageRegistrator.locatePeak
@@ -272,8 +283,13 @@ def run_reference(images, *, fp64=True, capture=False, **attrs):
                 cap["Cfilt"][(int(I), int(J))] = np.array(self._ImageRegistrator__C_filt)
 
             reg.locatePeak = types.MethodType(locate, reg)
-        with _stubs_installed(), contextlib.redirect_stdout(io.StringIO()), np.errstate(all="ignore"):
-            reg.alignImageStack()
+        cwd = os.getcwd()
+        os.chdir(td)
+        try:
+            with _stubs_installed(), contextlib.redirect_stdout(io.StringIO()), np.errstate(all="ignore"):
+                reg.alignImageStack()
+        finally:
+            os.chdir(cwd)
         if capture:
             reg._cap = cap
     return reg

@@ -720,11 +720,40 @@ def hotpix_filter(images, hotpixInfo, neighbourThres=0.01, dt=None):
 DEFAULTS = dict(shapePadded=[4096, 4096], fouCrop=[3072, 3072], triMode="diag", diagWidth=5, diagStart=0,
                 maxShift=100, subPixReg=16, Bmode="opti", Brad=512, weightMode="autologistic",
                 peaksigThres=6.0, logisticK=5.0, logisticNu=0.15, originMode="centroid",
-                suppressOrigin=True, shiftMethod="lanczos", doLazyFRC=True, filterMode=None,
+                suppressOrigin=True, shiftMethod="lanczos", doLazyFRC=True, doEvenOddFRC=False, filterMode=None,
                 doseFiltParam=[None, 0.24499, -1.6649, 2.8141, 32, 0], pixelsize=None, voltage=300.0,
                 hotpixInfo={"logisticK": 6.0, "relax": 0.925, "maxSigma": 8.0, "psf": "K2",
                             "guessHotpix": 0, "guessDeadpix": 0, "decorrOutliers": False,
                             "cutoffLower": -4.0, "cutoffUpper": 3.25, "neighborPix": 0})
+
+
+def even_odd_frc(aligned, o, fp64=True, workers=1):
+    """Independent half-set FRC.  zorro.py:2099-2224 (xcorr='tri').
+
+    The even and odd frames of the aligned stack are registered again by two
+    registrators with the parent's settings (its hot-pixel filter included;
+    their own FRC and dose filter produce nothing that is kept, so they are
+    not run), the two sums are aligned to each other with triMode 'first',
+    and tiledFRC runs on that pair with the crop limits of
+    hstack([transEven, transOdd]).  The sub-registrators do not recurse
+    (doEvenOddFRC=False: the reference's own sub-registrators inherit
+    doEvenOddFRC=True from the saved config and recurse until a half-set is
+    too small for cdfLogisticCurve).  Returns FRC (full ring count), FRC2D,
+    transEven, transOdd."""
+    sub = dict(o)
+    sub["doEvenOddFRC"] = False
+    sub["doLazyFRC"] = False
+    hot = "hot" in (o.get("filterMode") or "").lower()
+    sub["filterMode"] = "hot" if hot else None
+    ev = align_image_stack(aligned[0::2], fp64=fp64, workers=workers, **dict(sub, hotpixInfo=dict(o["hotpixInfo"])))
+    od = align_image_stack(aligned[1::2], fp64=fp64, workers=workers, **dict(sub, hotpixInfo=dict(o["hotpixInfo"])))
+    dt = Dtypes(fp64, workers)
+    pair = np.stack([ev["imageSum"], od["imageSum"]]).astype(dt.f)
+    eo = align_image_stack(pair, fp64=fp64, workers=workers,
+                           **dict(sub, triMode="first", hotpixInfo=dict(o["hotpixInfo"])))
+    trans = np.hstack([ev["translations"], od["translations"]])
+    frc, frc2d, _ = tiled_frc(eo["images"][0], eo["images"][1], trans, dt=dt)
+    return frc, frc2d, ev["translations"], od["translations"]
 
 
 def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
@@ -770,7 +799,10 @@ def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
     t, imageSum = apply_shifts(images, translations, o["originMode"], o["shiftMethod"], o["subPixReg"])
     bench["shifts1"] = time.time()
     res.update({"translations": t, "imageSum": imageSum, "errorDict": ed, "images": images})
-    if o["doLazyFRC"]:
+    if o["doEvenOddFRC"]:
+        frc, frc2d, te, to = even_odd_frc(images, o, fp64=fp64, workers=workers)
+        res.update({"FRC": frc, "FRC2D": frc2d, "transEven": te, "transOdd": to})
+    elif o["doLazyFRC"]:
         frc, frc2d, tiles = lazy_frc(images, t, dt=dt)
         res.update({"FRC": frc, "FRC2D": frc2d, "frc_tiles": tiles})
     bench["frc1"] = time.time()

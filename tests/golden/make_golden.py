@@ -40,6 +40,12 @@ CASES = {
     "frc_800": dict(movie=dict(n_frames=6, shape=(800, 800), seed=5, mean_dose=1.0, drift_sigma=1.2),
                     attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[1024, 1024], maxShift=30,
                                pixelsize=0.1, filterMode="dose", doseFiltParam=DOSE)),
+    # independent half-set FRC: even/odd frames re-registered (with the hot-pixel
+    # filter), the two sums aligned in 'first' mode, tiled FRC of the pair
+    "evenodd_frc": dict(movie=dict(n_frames=16, shape=(800, 780), seed=21, mean_dose=1.5, drift_sigma=1.0,
+                                   dtype="uint8", gain_map=True, hot_fraction=1e-3),
+                        attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[512, 512], maxShift=30,
+                                   pixelsize=0.1, filterMode="hot", doEvenOddFRC=True)),
     # template mode: correlate everything to frame 0, no solver
     "first_mode": dict(movie=dict(n_frames=5, shape=(120, 128), seed=21, mean_dose=3.0, drift_sigma=1.0),
                        attrs=dict(triMode="first", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=16,
@@ -87,6 +93,9 @@ def main(names=None):
             subset("FRC2D", reg.FRC2D, out)
         if reg.filtSum is not None:
             subset("filtSum", reg.filtSum, out)
+        if attrs.get("doEvenOddFRC"):
+            out["transEven"] = np.asarray(reg.transEven, dtype=np.float64)
+            out["transOdd"] = np.asarray(reg.transOdd, dtype=np.float64)
         if "hot" in (attrs.get("filterMode") or ""):
             for k in ("guessDeadpix", "guessHotpix", "neighborPix", "cutoffLower", "cutoffUpper",
                       "frameMean", "frameStd"):

@@ -186,11 +186,13 @@ def test_hot_pixels_and_gain():
 def test_golden_fixtures():
     """Against the unmodified reference's own outputs (tests/golden)."""
     from tests.golden.make_golden import CASES as GC, input_checksum
+    skipped = []
     for name, case in sorted(GC.items()):
         g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")))
         mv = make_movie(**case["movie"])
         if input_checksum(mv["images"]) != str(g["checksum"]):
-            pytest.skip("synthetic input differs on this platform")
+            skipped.append(name)  # the synthetic input differs on this platform
+            continue
         attrs = dict(case["attrs"])
         if case["movie"].get("dtype") == "uint8":
             reg = gpu_align(mv["raw"], gain=mv["gain"], **attrs)
@@ -213,3 +215,25 @@ def test_golden_fixtures():
             for k in ("guessDeadpix", "guessHotpix", "neighborPix"):
                 assert reg.hotpixInfo[k] == ref["hotpixInfo"][k], (name, k)
                 assert abs(reg.hotpixInfo[k] - int(g["hot_" + k])) <= 1 + 0.01 * int(g["hot_" + k]), (name, k)
+    if len(skipped) == len(GC):
+        pytest.skip("synthetic inputs differ on this platform: %s" % skipped)
+
+
+def test_even_odd_frc_against_oracle():
+    """Independent half-set FRC (doEvenOddFRC): 40 frames, so that each half
+    (20 frames, 190 pairs) has a well-posed weight fit; the half-set
+    trajectories within 0.01 px and the FRC within 1e-3 of the float64
+    oracle."""
+    mv = make_movie(n_frames=40, shape=(800, 780), seed=31, mean_dose=1.5, drift_sigma=0.8, dtype="uint8",
+                    gain_map=True, hot_fraction=1e-4)
+    attrs = dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[256, 256], maxShift=20, pixelsize=0.1,
+                 filterMode="hot", doEvenOddFRC=True)
+    reg = gpu_align(mv["raw"], gain=mv["gain"], **attrs)
+    ref = zo.align_image_stack(mv["images"], **attrs)
+    assert np.abs(reg.translations - ref["translations"]).max() <= TRAJ_TOL
+    assert np.abs(reg.transEven - ref["transEven"]).max() <= TRAJ_TOL
+    assert np.abs(reg.transOdd - ref["transOdd"]).max() <= TRAJ_TOL
+    assert reg.FRC.shape == ref["FRC"].shape
+    assert not np.all(np.isnan(ref["FRC"]))
+    assert np.nanmax(np.abs(np.asarray(reg.FRC) - ref["FRC"])) <= FRC_TOL
+    assert np.array_equal(np.isnan(np.asarray(reg.FRC)), np.isnan(ref["FRC"]))

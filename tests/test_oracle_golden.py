@@ -73,6 +73,14 @@ def test_sums_frc_dose(case):
         np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-6)
 
 
+def test_half_set_translations(case):
+    name, g, res, _ = case
+    if "transEven" not in g:
+        pytest.skip("no independent half-set FRC in this case")
+    np.testing.assert_allclose(res["transEven"], g["transEven"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(res["transOdd"], g["transOdd"], rtol=0, atol=1e-9)
+
+
 def test_hot_pixel_counts(case):
     name, g, res, _ = case
     if "hot_guessHotpix" not in g:

@@ -100,7 +100,7 @@ class Engine:
             st = self._slots.get(slot)
             if st is None:
                 stream = None if slot == 0 else self.torch.cuda.Stream(device=self.dev)
-                st = self._slots[slot] = {"bufs": {}, "stream": stream}
+                st = self._slots[slot] = {"bufs": {}, "stream": stream, "key": slot}
             return st
 
     @property
@@ -170,6 +170,7 @@ class Engine:
         the buffer pool and stream; one thread per slot at a time."""
         torch = self.torch
         st = self._slot(slot)
+        prev = getattr(self._tls, "slot", None)  # a half-set registration runs inside its parent's
         self._tls.slot = st
         try:
             sctx = torch.cuda.stream(st["stream"]) if st["stream"] is not None else contextlib.nullcontext()
@@ -178,9 +179,70 @@ class Engine:
                 if st["stream"] is not None:
                     st["stream"].synchronize()
         finally:
-            self._tls.slot = None
+            self._tls.slot = prev
         for k, v in res.items():
             setattr(reg, k, v)
+
+    def _even_odd_frc(self, reg, aligned, hotinfo, filt):
+        """Independent half-set FRC (evenOddFouRingCorr, zorro.py:2099-2224,
+        xcorr='tri').  The even and odd frames of the aligned stack are
+        registered again with the parent's settings (its hot-pixel filter
+        included; their own FRC and dose filter would produce nothing that is
+        kept, so they are not run), their sums are aligned to each other in
+        triMode 'first', and the tiled FRC of that pair uses the crop limits
+        of hstack([transEven, transOdd]).  The half-set registrators do not
+        recurse (the reference's own inherit doEvenOddFRC=True from the saved
+        config and recurse until a half-set is too small to fit).  Returns
+        FRC (all rings), FRC2D, transEven, transOdd."""
+        from .registrator import ImageRegistrator, copy_config
+        torch = self.torch
+        N, H, W = (int(v) for v in aligned.shape)
+        if N < 2:
+            raise ValueError("doEvenOddFRC needs at least two frames")
+        # the half-set registrations read the aligned stack on their own stream
+        torch.cuda.current_stream(self.dev).synchronize()
+        parent = self._tls.slot["key"]
+        sub_slot = ("halfset", parent)
+
+        def register(images, **kw):
+            r = ImageRegistrator()
+            copy_config(reg, r)
+            r.images = images
+            r.gainRef = None
+            r.masks = None
+            r.gain = None
+            r.doEvenOddFRC = False
+            r.doLazyFRC = False
+            r.filterMode = "hot" if "hot" in filt else None
+            r.hotpixInfo = dict(hotinfo)
+            r.keepAlignedImages = False
+            r.returnDeviceArrays = True
+            r.errorDictList = []
+            r.bench = {}
+            for k, v in kw.items():
+                setattr(r, k, v)
+            self.align(r, slot=sub_slot)
+            return r
+
+        ev = register(aligned[0::2])
+        od = register(aligned[1::2])
+        eo = register(torch.stack([ev.imageSum, od.imageSum]), triMode="first", keepAlignedImages=True)
+        te, to = np.asarray(ev.translations), np.asarray(od.translations)
+        box = 512
+        offs, tiles = hm.frc_tiles((H, W), np.hstack([te, to]))
+        nr = int(np.ceil(np.sqrt(2.0 * (box // 2) ** 2))) + 1
+        if len(offs) and (offs.min() < 0 or (offs[:, 0] + box).max() > H or (offs[:, 1] + box).max() > W):
+            raise ValueError("tiledFRC: tiles %s leave the %dx%d image (negative crop limits)" % (tiles, H, W))
+        if len(offs) == 0:
+            return np.full(nr, np.nan), np.full((box, box), np.nan, dtype=np.float32), te, to
+        pair = eo.images.contiguous()
+        offs_dev = torch.from_numpy(offs.reshape(-1)).to(self.dev, non_blocking=True)
+        fwb = self.lib.zr_frc_work_bytes(len(offs), box)
+        f2 = self.tensor("frc2d", (box, box), torch.float32)
+        fr = self.tensor("frc_eo", (nr,), torch.float64)
+        self.call("H_frc", "zr_tiled_frc", pair[0].data_ptr(), pair[1].data_ptr(), H, W, box, offs_dev.data_ptr(),
+                  len(offs), f2.data_ptr(), fr.data_ptr(), nr, self.ptr("frcwork", fwb), fwb, self.stream)
+        return fr, f2, te, to
 
     def _frames(self, raw, rtype, gain, ha=None, hb=None, gdiv=0.0):
         N, H, W = raw.shape
@@ -409,7 +471,8 @@ class Engine:
         isum = self.tensor("isum", (H, W), torch.float32)
         esum = self.tensor("esum", (H, W), torch.float32)
         osum = self.tensor("osum", (H, W), torch.float32)
-        need_aligned = reg.keepAlignedImages or any(f in ("dose", "dosenorm") for f in filt)
+        need_aligned = (reg.keepAlignedImages or bool(reg.doEvenOddFRC) or
+                        any(f in ("dose", "dosenorm") for f in filt))
         aligned = self.tensor("aligned", (N, H, W), torch.float32) if need_aligned else None
         self.call("G_shift_sum", "zr_shift_sum", C.byref(frames), sh_dev.data_ptr(), isum.data_ptr(), esum.data_ptr(),
                   osum.data_ptr(), aligned.data_ptr() if aligned is not None else None, st)
@@ -418,8 +481,8 @@ class Engine:
         # ---- lazy FRC (zorro.py:2226-2310)
         frc = frc2d = None
         if reg.doEvenOddFRC:
-            raise ValueError("doEvenOddFRC (independent half-set FRC) is not supported by the GPU path yet")
-        if reg.doLazyFRC:
+            frc, frc2d, out["transEven"], out["transOdd"] = self._even_odd_frc(reg, aligned, hotinfo, filt)
+        elif reg.doLazyFRC:
             offs, tiles = hm.frc_tiles((H, W), translations)
             box = 512
             if len(offs) and (offs.min() < 0 or (offs[:, 0] + box).max() > H or (offs[:, 1] + box).max() > W):
@@ -461,10 +524,20 @@ class Engine:
         out["translations"] = translations
         dev_out = bool(getattr(reg, "returnDeviceArrays", False))
 
+        # host results go through pinned buffers from torch's caching host
+        # allocator: all copies are queued on the stream, then one wait; each
+        # returned array keeps its pinned block alive
+        pending = []
+
         def fetch(t):
             if isinstance(t, np.ndarray):
                 return t
-            return t.clone() if dev_out else t.cpu().numpy().copy()
+            if dev_out:
+                return t.clone()
+            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+            h.copy_(t, non_blocking=True)
+            pending.append(h)
+            return h
 
         out["imageSum"] = fetch(isum)
         if frc is not None:
@@ -474,6 +547,11 @@ class Engine:
             out["filtSum"] = fetch(filt_sum)
         if reg.keepAlignedImages:
             out["images"] = fetch(aligned)
+        if pending:
+            torch.cuda.current_stream(self.dev).synchronize()
+            for k in ("imageSum", "FRC", "FRC2D", "filtSum", "images"):
+                if k in out and isinstance(out[k], torch.Tensor):
+                    out[k] = out[k].numpy()
         out["hotpixInfo"] = hotinfo
         out["shapeOriginal"] = [H, W]
         out["masks"] = np.ones([1, H, W], dtype=bool) if not user_mask else reg.masks

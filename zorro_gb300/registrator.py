@@ -73,6 +73,8 @@ class ImageRegistrator:
         self.doEvenOddFRC = False
         self.FRC = None
         self.FRC2D = None
+        self.transEven = None   # half-set trajectories of doEvenOddFRC
+        self.transOdd = None
         self.CTFProgram = None
         self.shapePadded = [4096, 4096]
         self.shapeOriginal = None
