@@ -14,8 +14,12 @@ absent or unbuildable here:
   and ``zorro_plotting`` (plotting and file I/O only);
 * ``pyfftw.builders.fft2/ifft2`` stand-ins on ``scipy.fft`` with the
   ``update_arrays``/``execute`` protocol the reference uses
-  (``zorro_util.py:1041,1047``); pyFFTW's default ``normalise_idft=True``
-  matches ``scipy.fft.ifft2``'s 1/N scaling;
+  (``zorro_util.py:1041,1047``).  The reference always runs its plans with
+  ``FFTW.execute()``, which applies no scaling in either direction (pyFFTW
+  applies ``normalise_idft`` only in ``FFTW.__call__``); the reference's own
+  factors (``normConst2`` in mnxc2, ``normConst`` in applyShifts and
+  binStack) are written for those unscaled inverses, so the stand-in's
+  inverse is unscaled too (``norm="forward"``);
 * a ``numexprz.evaluate`` stand-in that evaluates the expression string with
   NumPy on the caller's frame (the reference's 60 ``nz.evaluate`` sites);
 * ``np.int``/``np.float``/``np.Inf`` aliases removed in NumPy 2;
@@ -114,8 +118,11 @@ class _Plan:
         self.i, self.o = i, o
 
     def execute(self):
-        f = scipy.fft.ifft2 if self.inverse else scipy.fft.fft2
-        self.o[...] = f(self.i, workers=self.workers)
+        # FFTW.execute(): the plain transform, no 1/N on the inverse
+        if self.inverse:
+            self.o[...] = scipy.fft.ifft2(self.i, norm="forward", workers=self.workers)
+        else:
+            self.o[...] = scipy.fft.fft2(self.i, workers=self.workers)
 
 
 def _make_stubs(workers):

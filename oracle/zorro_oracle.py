@@ -44,7 +44,9 @@ class Dtypes:
         return scipy.fft.fft2(a.astype(self.c, copy=False), workers=self.workers)
 
     def ifft2(self, a):
-        return scipy.fft.ifft2(a, workers=self.workers)
+        """The inverse as the reference's FFTW plans run it (execute():
+        unscaled; its normConst factors account for that)."""
+        return scipy.fft.ifft2(a, norm="forward", workers=self.workers)
 
 
 # --------------------------------------------------------------------------

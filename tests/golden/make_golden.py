@@ -42,10 +42,10 @@ CASES = {
                                pixelsize=0.1, filterMode="dose", doseFiltParam=DOSE)),
     # independent half-set FRC: even/odd frames re-registered (with the hot-pixel
     # filter), the two sums aligned in 'first' mode, tiled FRC of the pair
-    "evenodd_frc": dict(movie=dict(n_frames=16, shape=(800, 780), seed=21, mean_dose=1.5, drift_sigma=1.0,
-                                   dtype="uint8", gain_map=True, hot_fraction=1e-3),
-                        attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[512, 512], maxShift=30,
-                                   pixelsize=0.1, filterMode="hot", doEvenOddFRC=True)),
+    # (40 frames: each half has 190 pairs, enough for a well-posed weight fit)
+    "evenodd_frc": dict(movie=dict(n_frames=40, shape=(800, 780), seed=21, mean_dose=1.5, drift_sigma=0.8),
+                        attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[512, 512], maxShift=20,
+                                   pixelsize=0.1, doEvenOddFRC=True)),
     # template mode: correlate everything to frame 0, no solver
     "first_mode": dict(movie=dict(n_frames=5, shape=(120, 128), seed=21, mean_dose=3.0, drift_sigma=1.0),
                        attrs=dict(triMode="first", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=16,

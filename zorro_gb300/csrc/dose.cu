@@ -339,7 +339,8 @@ extern "C" int zr_dose_filter(const float* aligned, int N, int H, int W, const z
                                                 tw, st))));
   }
   ZR_DOSE_DISPATCH(P0, ZR_TRY((dose_icols<LL>(ACC, FM, params->normalize, K4, H, T2, tw, st))));
-  const float scale = (float)(1.0 / ((double)P0 * P1));
+  // abs(IFFT2.execute(...)) at zorro.py:2484-2488: FFTW's inverse carries no 1/N
+  const float scale = 1.0f;
   ZR_DOSE_DISPATCH(P1, ZR_TRY((dose_irows<LL>(T2, K4, H, W, scale, filt_sum, tw, st))));
   return ZR_OK;
 }

@@ -600,7 +600,8 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
         Tx[fyi * L + nx] = acc;
       }
       __syncthreads();
-      const float invL2 = 1.0f / ((float)L * (float)L);
+      // |.| of the unscaled inverse (the reference's subIFFT2.execute(),
+      // zorro.py:1199), so corr = max / 16^2 carries its scale
       float bv = -INFINITY;
       int bi = 0x7fffffff;
       for (int e = threadIdx.x; e < L * L; e += PK_T) {
@@ -611,7 +612,7 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
           const float2 t = Wl[(fy * ny) & (L - 1)];
           acc = cadd(acc, cmul(Tx[fyi * L + nx], t));
         }
-        const float mag = sqrtf(acc.x * acc.x + acc.y * acc.y) * invL2;
+        const float mag = sqrtf(acc.x * acc.x + acc.y * acc.y);
         if (mag > bv || (mag == bv && e < bi)) { bv = mag; bi = e; }
       }
       block_argmax(sh, bv, bi);

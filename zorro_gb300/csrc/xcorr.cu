@@ -12,7 +12,8 @@
 //                values), inverse FFT of length C0, keep the w window rows;
 //   row pass     two window rows packed into one complex inverse FFT of length
 //                C1 (real-output trick), keep the w window columns, scale by
-//                normConst2 / (C0*C1) (zorro.py:634 and numpy's 1/N).
+//                normConst2 (zorro.py:634; the inverse, like the reference's
+//                FFTW execute(), carries no 1/N).
 //
 // The four frame-only terms (CorrTM, CorrBM and the two Denominator IFFTs)
 // depend on one frame each, so they are computed once per frame (zr_xcorr_terms)
@@ -241,8 +242,9 @@ static int run_jobs(XcJobs J, int njobs, int C0, int C1, int mS, const float* te
   const int wave = (int)((work_bytes / per_job) < (size_t)njobs ? work_bytes / per_job : (size_t)njobs);
   const float2* tw = twiddles();
   if (!tw) return ZR_ECUDA;
-  const double nc2 = (double)(float)(1.0 / (((double)C0 * C1) * ((double)C0 * C1)));
-  const float scale = (float)(nc2 / ((double)C0 * C1));
+  // normConst2 (zorro.py:634, rounded to float32 as there); the reference's
+  // inverse FFTs are FFTW executions without 1/N, and so is this one
+  const float scale = (float)(1.0 / (((double)C0 * C1) * ((double)C0 * C1)));
   float2* Tw = (float2*)work;
   for (int j0 = 0; j0 < njobs; j0 += wave) {
     const int nj = (njobs - j0) < wave ? (njobs - j0) : wave;
