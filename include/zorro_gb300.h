@@ -204,6 +204,20 @@ int zr_xcorr_pairs(const void* G, const float* terms, const int* pairs, int M, i
 int zr_xcorr_pairs_noalloc(const void* G, const float* terms, const int* pairs, int M, int N, int C0, int C1,
                            int max_shift, float* cwin, void* stream);
 
+/* triMode 'refine' (xcorrnm2_tri, zorro.py:934-954): frame I (I < N-1) is
+ * correlated with the template of all frames but I.
+ * zr_refine_spectra: templates[n] = (sum_m G[m] - G[n]) / N for every n (the
+ * reference's conj(sumFFT - baseImageFFT[I]) / N enters as A conj(B)).
+ * zr_refine_terms: the frame terms with CorrTM and DenomT of every slot n
+ * replaced by the template's, (sum_m term_m - term_n) / N (they are linear in
+ * the template spectra); out is [4N+1][w][w] like terms.
+ * zr_xcorr_refine: the N-1 windows of frame I against template I, combined
+ * with refine_terms as mnxc2 combines any pair; cwin is [N-1][w][w]. */
+int zr_refine_spectra(const void* G, int N, int C0, int C1, void* templates, void* stream);
+int zr_refine_terms(const float* terms, int N, int max_shift, float* out, void* stream);
+int zr_xcorr_refine(const void* G, const void* templates, const float* refine_terms, int N, int C0, int C1,
+                    int max_shift, float* cwin, void* work, size_t work_bytes, void* stream);
+
 /* ---- peak search: locatePeak, zorro.py:1099-1231 ---- */
 int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr_peak_params_t* params,
                     zr_peak_result_t* results, void* stream);

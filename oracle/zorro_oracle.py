@@ -216,9 +216,11 @@ def locate_peak(C, mask_maxShift, subPixReg=16, Bmode="opti", Brad=512, shapePad
 def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diagWidth=5, diagStart=0,
               maxShift=100, subPixReg=16, Bmode="opti", Brad=512, suppressOrigin=True, dt=None,
               capture=None, pairs_limit=None):
-    """All-pairs registration.  zorro.py:773-1011 (single mask, preShift off,
-    triMode not 'refine').  Returns (shiftsTriMat, corrTriMat, peaksigTriMat,
-    originTriMat)."""
+    """All-pairs registration.  zorro.py:773-1011 (single mask, preShift
+    off).  triMode 'refine' (zorro.py:934-954) correlates each frame I < N-1
+    with the template conj(sum_n G_n - G_I) / N (and likewise for the squared
+    spectra), filling the diagonal.  Returns (shiftsTriMat, corrTriMat,
+    peaksigTriMat, originTriMat)."""
     N = images_padded.shape[0]
     tri = tri_indices(N, triMode, diagWidth, diagStart)
     if np.any(fouCrop):
@@ -237,7 +239,23 @@ def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diag
     peaksig = np.zeros([N, N], dtype=dt.f)
     origin = np.zeros([N, N], dtype=dt.f)
     done = 0
-    for I in np.unique(np.argwhere(np.sum(tri, axis=1) > 0)):
+    if triMode == "refine":
+        sumG = np.sum(np.stack(G), axis=0)
+        sumS = np.sum(np.stack(S), axis=0)
+        for I in range(N - 1):
+            # mnxc2 conjugates its template argument: conj((sum - G_I) / N)
+            # equals the reference's conj(sum - G_I) / N exactly
+            C, o = mnxc2((sumG - G[I]) / N, (sumS - S[I]) / N, G[I], S[I], GM, MP, nc2, maxShift, suppressOrigin,
+                         dt)
+            origin[I, I] = o
+            r = locate_peak(C, mmask, subPixReg, Bmode, Brad, shapePadded, dt)
+            shifts[I, I, :] = r["shift"]
+            corr[I, I] = r["corr"]
+            peaksig[I, I] = r["peaksig"]
+            if capture is not None:
+                capture[(int(I), int(I))] = {"C": C, "sigma": r["sigma"], "C_filt": r["C_filt"]}
+    pair_rows = [] if triMode == "refine" else np.unique(np.argwhere(np.sum(tri, axis=1) > 0))
+    for I in pair_rows:
         for J in np.unique(np.argwhere(tri[I, :])):
             C, o = mnxc2(G[I], S[I], G[J], S[J], GM, MP, nc2, maxShift, suppressOrigin, dt)
             origin[I, J] = o
@@ -448,11 +466,17 @@ def lanczos_kernel(subPixShift, kernelShape=3, lobes=None):
     return k / np.sum(k)
 
 
-def apply_shifts(images, translations, originMode="centroid", shiftMethod="lanczos", subPixReg=16):
+def apply_shifts(images, translations, originMode="centroid", shiftMethod="lanczos", subPixReg=16, shapePadded=None,
+                 dt=None):
     """Shift every frame and sum.  zorro.py:1734-1808 with
     zorro_util.py:341-379 (lanczosIndexedShift).  ``images`` is modified in
-    place; returns (translations_applied, imageSum)."""
-    t = np.array(translations, dtype=np.float64, copy=True)
+    place; returns (translations_applied, imageSum).  (shiftMethod 'fourier'
+    never gets here: see align_image_stack.)"""
+    # the reference keeps the translations' dtype (float32 after 'refine',
+    # zorro.py:1643), and with it the precision of the centroid
+    t = np.array(translations, copy=True)
+    if not np.issubdtype(t.dtype, np.floating):
+        t = t.astype(np.float64)
     if originMode == "centroid":
         t -= np.mean(t, axis=0)
     if subPixReg > 1.0 and shiftMethod == "lanczos":
@@ -779,6 +803,11 @@ def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
         bench["hot1"] = time.time()
     N, H, W = images.shape
     P = o["shapePadded"]
+    if o["shiftMethod"] == "fourier":
+        # xcorrnm2_tri stores full spectra for this shift method and stops on
+        # an undefined attribute while doing so (self.__sC2, zorro.py:891-895)
+        raise AttributeError("shiftMethod 'fourier' is broken in the reference: self.__sC2 is undefined "
+                             "(zorro.py:895)")
     padded, mask = pad_stack(images, P)
     bench["xcorr0"] = time.time()
     sh, co, ps, orig = xcorr_tri(padded, mask, shapePadded=P, fouCrop=o["fouCrop"], triMode=o["triMode"],
@@ -790,6 +819,13 @@ def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
         translations = -sh[0, :]
         ed = {"shiftsTriMat": sh, "corrTriMat": co, "originTriMat": orig, "peaksigTriMat": ps,
               "translations": translations.copy()}
+    elif o["triMode"] == "refine":
+        # zorro.py:1635-1647: the diagonal, negated, in a float32 array
+        translations = np.zeros([N, 2], dtype="float32")
+        for K in range(N):
+            translations[K, :] = -sh[K, K, :]
+        ed = {"shiftsTriMat": sh, "corrTriMat": co, "originTriMat": orig, "peaksigTriMat": ps,
+              "translations": translations.copy()}
     else:
         ed = shifts_solver(sh, co, ps, shapeImage=P, maxShift=o["maxShift"], weightMode=o["weightMode"],
                            peaksigThres=o["peaksigThres"], logisticK=o["logisticK"],
@@ -798,7 +834,8 @@ def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
         translations = ed["translations"].copy()
     bench["solve1"] = time.time()
     images = padded[:, :H, :W]
-    t, imageSum = apply_shifts(images, translations, o["originMode"], o["shiftMethod"], o["subPixReg"])
+    t, imageSum = apply_shifts(images, translations, o["originMode"], o["shiftMethod"], o["subPixReg"],
+                               shapePadded=P, dt=dt)
     bench["shifts1"] = time.time()
     res.update({"translations": t, "imageSum": imageSum, "errorDict": ed, "images": images})
     if o["doEvenOddFRC"]:

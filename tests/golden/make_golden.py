@@ -46,6 +46,10 @@ CASES = {
     "evenodd_frc": dict(movie=dict(n_frames=40, shape=(800, 780), seed=21, mean_dose=1.5, drift_sigma=0.8),
                         attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[512, 512], maxShift=20,
                                    pixelsize=0.1, doEvenOddFRC=True)),
+    # refine mode: each frame against the sum of the others, no solver
+    "refine_mode": dict(movie=dict(n_frames=10, shape=(200, 180), seed=12, mean_dose=1.5, drift_sigma=0.8),
+                        attrs=dict(triMode="refine", shapePadded=[256, 256], fouCrop=[128, 128], maxShift=20,
+                                   pixelsize=0.1, doLazyFRC=False)),
     # template mode: correlate everything to frame 0, no solver
     "first_mode": dict(movie=dict(n_frames=5, shape=(120, 128), seed=21, mean_dose=3.0, drift_sigma=1.0),
                        attrs=dict(triMode="first", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=16,

@@ -236,3 +236,28 @@ def test_even_odd_frc_against_oracle():
     assert not np.all(np.isnan(ref["FRC"]))
     assert np.nanmax(np.abs(np.asarray(reg.FRC) - ref["FRC"])) <= FRC_TOL
     assert np.array_equal(np.isnan(np.asarray(reg.FRC)), np.isnan(ref["FRC"]))
+
+
+def test_fourier_shift_raises_like_the_reference():
+    """shiftMethod 'fourier' stops the reference in xcorrnm2_tri
+    (AttributeError, zorro.py:895); the GPU path refuses it the same way."""
+    mv = make_movie(n_frames=4, shape=(120, 112), seed=2, mean_dose=2.0, drift_sigma=0.5)
+    with pytest.raises(AttributeError):
+        gpu_align(mv["images"].copy(), triMode="tri", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=16,
+                  pixelsize=0.1, shiftMethod="fourier")
+    with pytest.raises(AttributeError):
+        zo.align_image_stack(mv["images"], triMode="tri", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=16,
+                             pixelsize=0.1, shiftMethod="fourier", weightMode="autologistic")
+
+
+def test_refine_mode_against_oracle():
+    """triMode 'refine': every frame against the sum of the others."""
+    mv = make_movie(n_frames=12, shape=(240, 256), seed=8, mean_dose=1.5, drift_sigma=0.7)
+    attrs = dict(triMode="refine", shapePadded=[256, 256], fouCrop=[256, 256], maxShift=24, pixelsize=0.1)
+    reg = gpu_align(mv["images"].copy(), **attrs)
+    ref = zo.align_image_stack(mv["images"], **attrs)
+    ed, eo = reg.errorDictList[-1], ref["errorDict"]
+    d = np.abs(np.diagonal(ed["shiftsTriMat"], axis1=0, axis2=1) - np.diagonal(eo["shiftsTriMat"], axis1=0, axis2=1))
+    assert np.mean(d.max(axis=0) < 1e-9) >= 0.9, d
+    assert np.abs(reg.translations - ref["translations"]).max() <= 1.0 / 16 + 1e-6
+    assert rel_l2(reg.imageSum, ref["imageSum"]) <= 1e-3

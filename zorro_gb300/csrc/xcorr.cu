@@ -42,8 +42,9 @@ struct XcJobs {
   const float2* S;
   const float2* GM;
   const int* pairs;  // kind 1
+  const float2* G2;  // kind 2: template spectra (triMode 'refine')
   int N;
-  int kind;          // 0 terms, 1 pairs
+  int kind;          // 0 terms, 1 pairs, 2 frame I against template I
   int job0;
   long long se;      // spectrum elements
   int rows;          // window rows kept by the column pass: w + 1 (terms) or w (pairs)
@@ -54,6 +55,11 @@ __device__ __forceinline__ void job_operands(const XcJobs& J, int job, const flo
     const int I = J.pairs[2 * job], Jj = J.pairs[2 * job + 1];
     A = J.G + (size_t)Jj * J.se;
     B = J.G + (size_t)I * J.se;
+    return;
+  }
+  if (J.kind == 2) {  // base frame I, template (sum_n G_n - G_I) / N
+    A = J.G + (size_t)job * J.se;
+    B = J.G2 + (size_t)job * J.se;
     return;
   }
   const int t = job / J.N, n = job - t * J.N;
@@ -184,7 +190,8 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
         out[(size_t)refl_slot * w2 + (size_t)(w - a) * w + (w - b)] = v;
       }
     } else {
-      const int I = J.pairs[2 * job], Jj = J.pairs[2 * job + 1];
+      const int I = J.kind == 1 ? J.pairs[2 * job] : job;
+      const int Jj = J.kind == 1 ? J.pairs[2 * job + 1] : job;
       const int N = J.N;
       const float ctm = terms[(size_t)I * w2 + pix];
       const float cbm = terms[(size_t)(N + Jj) * w2 + pix];
@@ -263,9 +270,73 @@ static int check_sizes(int C0, int C1, int mS) {
   return ZR_OK;
 }
 
+// triMode 'refine' (zorro.py:934-954): template I is conj(sum_n G_n - G_I)/N.
+// One thread per spectrum element: the frame sum in frame order, then every
+// frame's template.
+__global__ void k_refine_spectra(const float2* __restrict__ G, int N, long long se, float2* __restrict__ T) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= se) return;
+  float sx = 0.0f, sy = 0.0f;
+  for (int n = 0; n < N; n++) {
+    const float2 g = G[(size_t)n * se + e];
+    sx += g.x;
+    sy += g.y;
+  }
+  const float fn = (float)N;
+  for (int n = 0; n < N; n++) {
+    const float2 g = G[(size_t)n * se + e];
+    T[(size_t)n * se + e] = make_float2((sx - g.x) / fn, (sy - g.y) / fn);
+  }
+}
+
+// The template's frame terms are linear in its spectra: CorrTM and the raw
+// DenomT of template I are (sum_n term_n - term_I) / N.  CorrBM, DenomB and
+// the mask product are copied.
+__global__ void k_refine_terms(const float* __restrict__ terms, int N, int w2, float* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= w2) return;
+  const float fn = (float)N;
+  for (int t = 0; t < 4; t += 2) {  // CorrTM (slots [0,N)) and DenomT (slots [2N,3N))
+    const float* src = terms + (size_t)t * N * w2;
+    float s = 0.0f;
+    for (int n = 0; n < N; n++) s += src[(size_t)n * w2 + p];
+    for (int n = 0; n < N; n++) out[((size_t)t * N + n) * w2 + p] = (s - src[(size_t)n * w2 + p]) / fn;
+  }
+  for (int n = 0; n < N; n++) {
+    out[((size_t)N + n) * w2 + p] = terms[((size_t)N + n) * w2 + p];
+    out[((size_t)3 * N + n) * w2 + p] = terms[((size_t)3 * N + n) * w2 + p];
+  }
+  out[(size_t)4 * N * w2 + p] = terms[(size_t)4 * N * w2 + p];
+}
+
 }  // namespace zr
 
 using namespace zr;
+
+extern "C" int zr_refine_spectra(const void* G, int N, int C0, int C1, void* templates, void* stream) {
+  if (!G || !templates || N <= 0) return set_error(ZR_EINVAL, "zr_refine_spectra: null argument");
+  const long long se = zr_spectrum_elems(C0, C1);
+  k_refine_spectra<<<(unsigned)((se + 255) / 256), 256, 0, (cudaStream_t)stream>>>((const float2*)G, N, se,
+                                                                                    (float2*)templates);
+  return launched("k_refine_spectra");
+}
+
+extern "C" int zr_refine_terms(const float* terms, int N, int max_shift, float* out, void* stream) {
+  if (!terms || !out || N <= 0 || max_shift <= 0) return set_error(ZR_EINVAL, "zr_refine_terms: bad argument");
+  const int w2 = 4 * max_shift * max_shift;
+  k_refine_terms<<<(w2 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(terms, N, w2, out);
+  return launched("k_refine_terms");
+}
+
+extern "C" int zr_xcorr_refine(const void* G, const void* templates, const float* refine_terms, int N, int C0,
+                               int C1, int max_shift, float* cwin, void* work, size_t work_bytes, void* stream) {
+  if (!G || !templates || !refine_terms || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_refine: null argument");
+  if (N < 2) return ZR_OK;
+  ZR_TRY(check_sizes(C0, C1, max_shift));
+  XcJobs J{(const float2*)G, nullptr, nullptr, nullptr, (const float2*)templates, N, 2, 0,
+           zr_spectrum_elems(C0, C1), 2 * max_shift};
+  return run_jobs(J, N - 1, C0, C1, max_shift, refine_terms, cwin, work, work_bytes, (cudaStream_t)stream);
+}
 
 extern "C" size_t zr_xcorr_work_bytes(int n_jobs, int C1, int max_shift) {
   return (size_t)n_jobs * (2 * max_shift + 1) * zr_spectrum_pitch(C1) * sizeof(float2);
@@ -275,8 +346,8 @@ extern "C" int zr_xcorr_terms(const void* G, const void* S, const void* GM, int 
                               float* terms, void* work, size_t work_bytes, void* stream) {
   if (!G || !S || !GM || !terms || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_terms: null argument");
   ZR_TRY(check_sizes(C0, C1, max_shift));
-  XcJobs J{(const float2*)G, (const float2*)S, (const float2*)GM, nullptr, N, 0, 0, zr_spectrum_elems(C0, C1),
-           2 * max_shift + 1};
+  XcJobs J{(const float2*)G, (const float2*)S, (const float2*)GM, nullptr, nullptr, N, 0, 0,
+           zr_spectrum_elems(C0, C1), 2 * max_shift + 1};
   return run_jobs(J, 2 * N + 1, C0, C1, max_shift, nullptr, terms, work, work_bytes, (cudaStream_t)stream);
 }
 
@@ -285,6 +356,6 @@ extern "C" int zr_xcorr_pairs(const void* G, const float* terms, const int* pair
   if (!G || !terms || !pairs || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_pairs: null argument");
   if (M <= 0) return ZR_OK;
   ZR_TRY(check_sizes(C0, C1, max_shift));
-  XcJobs J{(const float2*)G, nullptr, nullptr, pairs, N, 1, 0, zr_spectrum_elems(C0, C1), 2 * max_shift};
+  XcJobs J{(const float2*)G, nullptr, nullptr, pairs, nullptr, N, 1, 0, zr_spectrum_elems(C0, C1), 2 * max_shift};
   return run_jobs(J, M, C0, C1, max_shift, terms, cwin, work, work_bytes, (cudaStream_t)stream);
 }

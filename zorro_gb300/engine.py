@@ -257,8 +257,11 @@ class Engine:
         bench["align0"] = time.time()
         if reg.preShift:
             raise ValueError("preShift is not supported by the GPU path")
-        if reg.triMode == "refine":
-            raise ValueError("triMode 'refine' is not supported by the GPU path")
+        if reg.shiftMethod == "fourier":
+            # the reference stops in xcorrnm2_tri while storing the full spectra
+            # that shift method needs (self.__sC2 is undefined, zorro.py:891-895)
+            raise AttributeError("shiftMethod 'fourier' is broken in the reference: self.__sC2 is undefined "
+                                 "(zorro.py:895)")
         if reg.shapeBinned is not None and np.any(reg.shapeBinned):
             raise ValueError("shapeBinned (Fourier binning) is not supported by the GPU path yet")
         raw, gain, rtype = self.upload(reg)
@@ -367,18 +370,31 @@ class Engine:
                       G[f0].data_ptr(), S[f0].data_ptr(), wptr, wb, st)
 
         # ---- correlation windows and peaks (mnxc2 / locatePeak)
-        tri = hm.tri_indices(N, reg.triMode, reg.diagWidth, reg.diagStart)
-        pairs = hm.pair_list(tri)
+        refine = reg.triMode == "refine"
+        if refine:
+            # frame I against the template of the others, I < N-1 (zorro.py:941-954)
+            pairs = np.array([(I, I) for I in range(N - 1)], dtype=np.int32).reshape(-1, 2)
+        else:
+            tri = hm.tri_indices(N, reg.triMode, reg.diagWidth, reg.diagStart)
+            pairs = hm.pair_list(tri)
         M = len(pairs)
         terms = self.tensor("terms", (4 * N + 1, w, w), torch.float32)
         xw = min(XCORR_WORK, max(self.lib.zr_xcorr_work_bytes(1, C1, mS), self.lib.zr_xcorr_work_bytes(M, C1, mS)))
         xptr = self.ptr("xcwork", xw)
         self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), N, C0, C1, mS, terms.data_ptr(), xptr,
                   xw, st)
-        pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
         cwin = self.tensor("cwin", (max(M, 1), w, w), torch.float32)
-        self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pairs_dev.data_ptr(), M, N, C0, C1, mS,
-                  cwin.data_ptr(), xptr, xw, st)
+        if refine:
+            TG = self.tensor("refineT", (N, se, 2), torch.float32)
+            rterms = self.tensor("refine_terms", (4 * N + 1, w, w), torch.float32)
+            self.call("E_pairs", "zr_refine_spectra", G.data_ptr(), N, C0, C1, TG.data_ptr(), st)
+            self.call("E_pairs", "zr_refine_terms", terms.data_ptr(), N, mS, rterms.data_ptr(), st)
+            self.call("E_pairs", "zr_xcorr_refine", G.data_ptr(), TG.data_ptr(), rterms.data_ptr(), N, C0, C1, mS,
+                      cwin.data_ptr(), xptr, xw, st)
+        else:
+            pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
+            self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pairs_dev.data_ptr(), M, N, C0, C1,
+                      mS, cwin.data_ptr(), xptr, xw, st)
         pp = PeakParams()
         pp.sub_pix_reg = int(reg.subPixReg or 1)
         bm = str(reg.Bmode)
@@ -436,6 +452,13 @@ class Engine:
             translations = -shifts[0, :]
             ed = {"shiftsTriMat": shifts, "corrTriMat": corr, "originTriMat": orig, "peaksigTriMat": psig,
                   "translations": translations.copy()}
+        elif refine:
+            # zorro.py:1635-1647: the negated diagonal, in a float32 array
+            translations = np.zeros([N, 2], dtype="float32")
+            for K in range(N):
+                translations[K, :] = -shifts[K, K, :]
+            ed = {"shiftsTriMat": shifts, "corrTriMat": corr, "originTriMat": orig, "peaksigTriMat": psig,
+                  "translations": translations.copy()}
         else:
             ed = hm.solve_shifts(shifts, corr, psig, shapeImage=[P0, P1], maxShift=reg.maxShift,
                                  weightMode=reg.weightMode, peaksigThres=reg.peaksigThres, logisticK=reg.logisticK,
@@ -454,8 +477,6 @@ class Engine:
         if reg.originMode == "centroid":
             translations = translations - np.mean(translations, axis=0)
         if not (reg.subPixReg > 1.0 and reg.shiftMethod == "lanczos"):
-            if reg.subPixReg > 1.0 and reg.shiftMethod == "fourier":
-                raise ValueError("shiftMethod 'fourier' is not supported by the GPU path")
             # integer roll only (zorro.py:1790-1796)
             params = [(int(v[0]), int(v[1]), 0, np.array([0, 1.0, 0]), np.array([0, 1.0, 0]))
                       for v in np.round(translations).astype(int)]
