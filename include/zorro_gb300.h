@@ -204,6 +204,21 @@ int zr_xcorr_pairs(const void* G, const float* terms, const int* pairs, int M, i
 int zr_xcorr_pairs_noalloc(const void* G, const float* terms, const int* pairs, int M, int N, int C0, int C1,
                            int max_shift, float* cwin, void* stream);
 
+/* Half-precision spectra (the mixed-precision form of the path; the
+ * reference stores complex64): spectrum n of ``spectra`` ([n_spectra][se]
+ * complex float) is written to ``out`` as __half2 times scales[n], a power
+ * of two with max(|re|, |im|) * scales[n] < 2^15.  work: n_spectra * 4
+ * bytes.  The _half correlation passes read such spectra (G, S and GM with
+ * scales [N] G, [N] S, [1] GM; the pair pass uses the G scales), undo the
+ * scales exactly, and otherwise compute what zr_xcorr_terms / zr_xcorr_pairs
+ * compute, in float. */
+int zr_pack_half(const void* spectra, int n_spectra, long long se, void* out, float* scales, void* work,
+                 size_t work_bytes, void* stream);
+int zr_xcorr_terms_half(const void* G, const void* S, const void* GM, const float* scales, int N, int C0, int C1,
+                        int max_shift, float* terms, void* work, size_t work_bytes, void* stream);
+int zr_xcorr_pairs_half(const void* G, const float* scales, const float* terms, const int* pairs, int M, int N,
+                        int C0, int C1, int max_shift, float* cwin, void* work, size_t work_bytes, void* stream);
+
 /* triMode 'refine' (xcorrnm2_tri, zorro.py:934-954): frame I (I < N-1) is
  * correlated with the template of all frames but I.
  * zr_refine_spectra: templates[n] = (sum_m G[m] - G[n]) / N for every n (the

@@ -194,3 +194,24 @@ def test_hotpix_fit_bit_exact_over_random_histograms():
         assert mu == ref["mu"] and sg == ref["sigma"], t
         assert cu == ref["cutoffUpper"], t
         assert cl == ref["cutoffLower"] or (np.isnan(cl) and np.isnan(ref["cutoffLower"])), t
+
+
+@pytest.mark.parametrize("info", [{"Horizontal": True, "Vertical": True, "Diagonal": False},
+                                  {"Horizontal": True, "Vertical": False, "Diagonal": False},
+                                  {"Horizontal": False, "Vertical": True, "Diagonal": True},
+                                  {"Horizontal": False, "Vertical": False, "Diagonal": True}])
+def test_gain_reference_orientation(info):
+    """loadGainRef orients the gain reference as loadData does
+    (zorro.py:3486-3502)."""
+    from zorro_gb300.registrator import ImageRegistrator
+    g = np.arange(12, dtype=np.float32).reshape(3, 4)
+    want = np.rot90(g, 1) if info["Diagonal"] else g
+    if info["Horizontal"] and info["Vertical"]:
+        want = np.rot90(want, 2)
+    elif info["Horizontal"]:
+        want = want[:, ::-1]
+    elif info["Vertical"]:
+        want = want[::-1, :]
+    r = ImageRegistrator()
+    r.gainInfo = dict(info)
+    assert np.array_equal(r.loadGainRef(g), want)

@@ -20,7 +20,7 @@ EXPORTS = (
     "zr_spectra", "zr_xcorr_work_bytes", "zr_xcorr_terms", "zr_xcorr_pairs", "zr_locate_peaks",
     "zr_shift_sum", "zr_frc_work_bytes", "zr_tiled_frc", "zr_dose_work_bytes", "zr_dose_filter",
     "zr_l1_solve", "zr_xcorr_pairs_noalloc", "zr_logistic_fit", "zr_refine_spectra", "zr_refine_terms",
-    "zr_xcorr_refine",
+    "zr_xcorr_refine", "zr_pack_half", "zr_xcorr_terms_half", "zr_xcorr_pairs_half",
 )
 
 
@@ -86,6 +86,10 @@ _SIGS = {
     "zr_xcorr_terms": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, C.c_size_t, _P]),
     "zr_xcorr_pairs": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, C.c_size_t,
                                  _P]),
+    "zr_pack_half": (C.c_int, [_P, C.c_int, C.c_longlong, _P, _P, _P, C.c_size_t, _P]),
+    "zr_xcorr_terms_half": (C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, C.c_size_t, _P]),
+    "zr_xcorr_pairs_half": (C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P,
+                                      C.c_size_t, _P]),
     "zr_refine_spectra": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
     "zr_refine_terms": (C.c_int, [_P, C.c_int, C.c_int, _P, _P]),
     "zr_xcorr_refine": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, C.c_size_t, _P]),

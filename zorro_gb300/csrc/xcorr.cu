@@ -38,11 +38,12 @@ constexpr int XC_EPT = ZR_XC_EPT;
 constexpr int XC_NBR = 2;  // packed row pairs per CTA in the row pass
 
 struct XcJobs {
-  const float2* G;
-  const float2* S;
-  const float2* GM;
+  const void* G;     // spectra: float2, or __half2 when ``sc`` is set
+  const void* S;
+  const void* GM;
   const int* pairs;  // kind 1
-  const float2* G2;  // kind 2: template spectra (triMode 'refine')
+  const void* G2;    // kind 2: template spectra (triMode 'refine')
+  const float* sc;   // half spectra: power-of-two scales, [N] G, [N] S, [1] GM
   int N;
   int kind;          // 0 terms, 1 pairs, 2 frame I against template I
   int job0;
@@ -50,27 +51,47 @@ struct XcJobs {
   int rows;          // window rows kept by the column pass: w + 1 (terms) or w (pairs)
 };
 
-__device__ __forceinline__ void job_operands(const XcJobs& J, int job, const float2*& A, const float2*& B) {
+// The two spectra of a job (its product is A conj(B)) and, for half-precision
+// spectra, the factor 1 / (scale_A scale_B) that undoes their scaling.
+template <typename E>
+__device__ __forceinline__ void job_operands(const XcJobs& J, int job, const E*& A, const E*& B, float& unscale) {
+  const E* G = (const E*)J.G;
+  int ia = 0, ib = 0;  // scale slots
   if (J.kind == 1) {
     const int I = J.pairs[2 * job], Jj = J.pairs[2 * job + 1];
-    A = J.G + (size_t)Jj * J.se;
-    B = J.G + (size_t)I * J.se;
-    return;
+    A = G + (size_t)Jj * J.se;
+    B = G + (size_t)I * J.se;
+    ia = Jj;
+    ib = I;
+  } else if (J.kind == 2) {  // base frame I, template (sum_n G_n - G_I) / N
+    A = G + (size_t)job * J.se;
+    B = (const E*)J.G2 + (size_t)job * J.se;
+  } else {
+    const int t = job / J.N, n = job - t * J.N;
+    const E* GM = (const E*)J.GM;
+    switch (t) {
+      case 0: A = G + (size_t)n * J.se; B = GM; ia = n; break;                    // CorrBM (and CorrTM)
+      case 1: A = (const E*)J.S + (size_t)n * J.se; B = GM; ia = J.N + n; break;  // DenomB (and DenomT)
+      default: A = GM; B = GM; ia = 2 * J.N; break;                              // maskProduct
+    }
+    ib = 2 * J.N;
   }
-  if (J.kind == 2) {  // base frame I, template (sum_n G_n - G_I) / N
-    A = J.G + (size_t)job * J.se;
-    B = J.G2 + (size_t)job * J.se;
-    return;
-  }
-  const int t = job / J.N, n = job - t * J.N;
-  switch (t) {
-    case 0: A = J.G + (size_t)n * J.se; B = J.GM; break;   // CorrBM: conj(M) * G_n (and CorrTM)
-    case 1: A = J.S + (size_t)n * J.se; B = J.GM; break;   // DenomB: conj(M) * S_n (and DenomT)
-    default: A = J.GM; B = J.GM; break;                     // maskProduct
-  }
+  unscale = J.sc ? 1.0f / (J.sc[ia] * J.sc[ib]) : 1.0f;
 }
 
-template <int C0>
+// Two consecutive complex values of a spectrum column, and one value.
+__device__ __forceinline__ float4 load_pair(const float2* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ float4 load_pair(const __half2* p) {
+  const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ float2 load_one(const float2* p) { return *p; }
+__device__ __forceinline__ float2 load_one(const __half2* p) { return __half22float2(*p); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+template <int C0, typename E>
 __global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks(C0))
     k_xc_cols(XcJobs J, int C1, int K4, int mS, float2* __restrict__ Tw, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(C0, XC_NBC, XC_EPT);
@@ -80,8 +101,9 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks
   // share the same column tile of every spectrum through L2
   const int k0 = blockIdx.y * XC_NBC;
   const int jl = blockIdx.x;
-  const float2 *A, *B;
-  job_operands(J, J.job0 + jl, A, B);
+  const E *A, *B;
+  float us;
+  job_operands(J, J.job0 + jl, A, B, us);
   const int half = C1 / 2, hc = C0 / 2;
   const int RP = C0 + 4;  // column pitch of the spectra
   // two rows per element: 16-byte loads along each (contiguous) column.  The
@@ -99,8 +121,8 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks
         const int c = e / (C0 / 2), r = 2 * (e - c * (C0 / 2));
         const int k = k0 + c;
         if (k < half) {
-          av[u] = __ldg(reinterpret_cast<const float4*>(A + (size_t)k * RP + r));
-          bv[u] = __ldg(reinterpret_cast<const float4*>(B + (size_t)k * RP + r));
+          av[u] = load_pair(A + (size_t)k * RP + r);
+          bv[u] = load_pair(B + (size_t)k * RP + r);
         }
       }
     }
@@ -115,15 +137,19 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks
         h0 = cmulc(make_float2(av[u].x, av[u].y), make_float2(bv[u].x, bv[u].y));
         h1 = cmulc(make_float2(av[u].z, av[u].w), make_float2(bv[u].z, bv[u].w));
         if (k > 0 && r == hc) {
-          const float2 h2 = cmulc(A[(size_t)k * RP + C0], B[(size_t)k * RP + C0]);
+          const float2 h2 = cmulc(load_one(A + (size_t)k * RP + C0), load_one(B + (size_t)k * RP + C0));
           h0 = make_float2(0.5f * (h0.x + h2.x), 0.5f * (h0.y + h2.y));
         }
       } else if (k == half) {
-        const float2* Ak = A + (size_t)k * RP;
-        const float2* Bk = B + (size_t)k * RP;
+        const E* Ak = A + (size_t)k * RP;
+        const E* Bk = B + (size_t)k * RP;
         const int m0 = (r == 0) ? 0 : (r == hc ? C0 : C0 - r), m1 = C0 - r - 1;
-        h0 = cmulc(Bk[m0], Ak[m0]);  // conj(A) * B at the mirrored row
-        h1 = cmulc(Bk[m1], Ak[m1]);
+        h0 = cmulc(load_one(Bk + m0), load_one(Ak + m0));  // conj(A) * B at the mirrored row
+        h1 = cmulc(load_one(Bk + m1), load_one(Ak + m1));
+      }
+      if (sizeof(E) != sizeof(float2)) {  // undo the power-of-two scales (exact)
+        h0 = cscale(h0, us);
+        h1 = cscale(h1, us);
       }
       sm[c * LD + pidx(r)] = h0;
       sm[c * LD + pidx(r + 1)] = h1;
@@ -205,15 +231,22 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
   }
 }
 
+template <int C0, typename E>
+static int launch_xc_cols_t(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
+                            cudaStream_t st) {
+  constexpr int T = fft_threads(C0, XC_NBC, XC_EPT);
+  const size_t smem = (size_t)XC_NBC * ld_of(C0) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_xc_cols attr"));
+  k_xc_cols<C0, E><<<dim3(nj, K4 / XC_NBC), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
+  return launched("k_xc_cols");
+}
+
 template <int C0>
 static int launch_xc_cols(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
                           cudaStream_t st) {
-  constexpr int T = fft_threads(C0, XC_NBC, XC_EPT);
-  const size_t smem = (size_t)XC_NBC * ld_of(C0) * sizeof(float2);
-  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                    "k_xc_cols attr"));
-  k_xc_cols<C0><<<dim3(nj, K4 / XC_NBC), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
-  return launched("k_xc_cols");
+  if (J.sc) return launch_xc_cols_t<C0, __half2>(J, nj, C1, K4, mS, Tw, tw, st);
+  return launch_xc_cols_t<C0, float2>(J, nj, C1, K4, mS, Tw, tw, st);
 }
 
 template <int C1>
@@ -309,9 +342,59 @@ __global__ void k_refine_terms(const float* __restrict__ terms, int N, int w2, f
   out[(size_t)4 * N * w2 + p] = terms[(size_t)4 * N * w2 + p];
 }
 
+// Half-precision spectra: each spectrum is stored as __half2 times a power of
+// two chosen from its largest component, max * scale < 2^15.
+__global__ void k_spectrum_absmax(const float2* __restrict__ X, long long se, unsigned int* __restrict__ maxbits) {
+  const float2* x = X + (size_t)blockIdx.y * se;
+  float m = 0.0f;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < se; e += (long long)gridDim.x * blockDim.x) {
+    const float2 v = x[e];
+    m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits + blockIdx.y, __float_as_uint(m));  // m >= 0: bits order as values
+}
+
+__device__ __forceinline__ float half_scale(unsigned int bits) {
+  const float m = __uint_as_float(bits);
+  if (!(m > 0.0f) || isinf(m)) return 1.0f;
+  int ex;
+  frexpf(m, &ex);  // m < 2^ex
+  return ldexpf(1.0f, 15 - ex);
+}
+
+__global__ void k_spectrum_to_half(const float2* __restrict__ X, long long se, const unsigned int* __restrict__ maxbits,
+                                   __half2* __restrict__ Y, float* __restrict__ scales) {
+  const int n = blockIdx.y;
+  const float sc = half_scale(maxbits[n]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) scales[n] = sc;
+  const float2* x = X + (size_t)n * se;
+  __half2* y = Y + (size_t)n * se;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < se; e += (long long)gridDim.x * blockDim.x) {
+    const float2 v = x[e];
+    y[e] = __floats2half2_rn(v.x * sc, v.y * sc);
+  }
+}
+
 }  // namespace zr
 
 using namespace zr;
+
+extern "C" int zr_pack_half(const void* spectra, int n_spectra, long long se, void* out, float* scales, void* work,
+                            size_t work_bytes, void* stream) {
+  if (!spectra || !out || !scales || !work || n_spectra <= 0 || se <= 0)
+    return set_error(ZR_EINVAL, "zr_pack_half: bad argument");
+  if (work_bytes < (size_t)n_spectra * sizeof(unsigned int))
+    return set_error(ZR_EWORK, "zr_pack_half: work buffer %zu < %zu", work_bytes, (size_t)n_spectra * 4);
+  cudaStream_t st = (cudaStream_t)stream;
+  ZR_TRY(cuda_check(cudaMemsetAsync(work, 0, (size_t)n_spectra * sizeof(unsigned int), st), "zr_pack_half memset"));
+  const int blocks = (int)((se + 255) / 256 < 304 ? (se + 255) / 256 : 304);
+  k_spectrum_absmax<<<dim3(blocks, n_spectra), 256, 0, st>>>((const float2*)spectra, se, (unsigned int*)work);
+  ZR_TRY(launched("k_spectrum_absmax"));
+  k_spectrum_to_half<<<dim3(blocks, n_spectra), 256, 0, st>>>((const float2*)spectra, se, (const unsigned int*)work,
+                                                               (__half2*)out, scales);
+  return launched("k_spectrum_to_half");
+}
 
 extern "C" int zr_refine_spectra(const void* G, int N, int C0, int C1, void* templates, void* stream) {
   if (!G || !templates || N <= 0) return set_error(ZR_EINVAL, "zr_refine_spectra: null argument");
@@ -333,8 +416,7 @@ extern "C" int zr_xcorr_refine(const void* G, const void* templates, const float
   if (!G || !templates || !refine_terms || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_refine: null argument");
   if (N < 2) return ZR_OK;
   ZR_TRY(check_sizes(C0, C1, max_shift));
-  XcJobs J{(const float2*)G, nullptr, nullptr, nullptr, (const float2*)templates, N, 2, 0,
-           zr_spectrum_elems(C0, C1), 2 * max_shift};
+  XcJobs J{G, nullptr, nullptr, nullptr, templates, nullptr, N, 2, 0, zr_spectrum_elems(C0, C1), 2 * max_shift};
   return run_jobs(J, N - 1, C0, C1, max_shift, refine_terms, cwin, work, work_bytes, (cudaStream_t)stream);
 }
 
@@ -346,8 +428,7 @@ extern "C" int zr_xcorr_terms(const void* G, const void* S, const void* GM, int 
                               float* terms, void* work, size_t work_bytes, void* stream) {
   if (!G || !S || !GM || !terms || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_terms: null argument");
   ZR_TRY(check_sizes(C0, C1, max_shift));
-  XcJobs J{(const float2*)G, (const float2*)S, (const float2*)GM, nullptr, nullptr, N, 0, 0,
-           zr_spectrum_elems(C0, C1), 2 * max_shift + 1};
+  XcJobs J{G, S, GM, nullptr, nullptr, nullptr, N, 0, 0, zr_spectrum_elems(C0, C1), 2 * max_shift + 1};
   return run_jobs(J, 2 * N + 1, C0, C1, max_shift, nullptr, terms, work, work_bytes, (cudaStream_t)stream);
 }
 
@@ -356,6 +437,24 @@ extern "C" int zr_xcorr_pairs(const void* G, const float* terms, const int* pair
   if (!G || !terms || !pairs || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_pairs: null argument");
   if (M <= 0) return ZR_OK;
   ZR_TRY(check_sizes(C0, C1, max_shift));
-  XcJobs J{(const float2*)G, nullptr, nullptr, pairs, nullptr, N, 1, 0, zr_spectrum_elems(C0, C1), 2 * max_shift};
+  XcJobs J{G, nullptr, nullptr, pairs, nullptr, nullptr, N, 1, 0, zr_spectrum_elems(C0, C1), 2 * max_shift};
+  return run_jobs(J, M, C0, C1, max_shift, terms, cwin, work, work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int zr_xcorr_terms_half(const void* G, const void* S, const void* GM, const float* scales, int N, int C0,
+                                   int C1, int max_shift, float* terms, void* work, size_t work_bytes, void* stream) {
+  if (!G || !S || !GM || !scales || !terms || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_terms_half: null argument");
+  ZR_TRY(check_sizes(C0, C1, max_shift));
+  XcJobs J{G, S, GM, nullptr, nullptr, scales, N, 0, 0, zr_spectrum_elems(C0, C1), 2 * max_shift + 1};
+  return run_jobs(J, 2 * N + 1, C0, C1, max_shift, nullptr, terms, work, work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int zr_xcorr_pairs_half(const void* G, const float* scales, const float* terms, const int* pairs, int M,
+                                   int N, int C0, int C1, int max_shift, float* cwin, void* work, size_t work_bytes,
+                                   void* stream) {
+  if (!G || !scales || !terms || !pairs || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_pairs_half: null argument");
+  if (M <= 0) return ZR_OK;
+  ZR_TRY(check_sizes(C0, C1, max_shift));
+  XcJobs J{G, nullptr, nullptr, pairs, nullptr, scales, N, 1, 0, zr_spectrum_elems(C0, C1), 2 * max_shift};
   return run_jobs(J, M, C0, C1, max_shift, terms, cwin, work, work_bytes, (cudaStream_t)stream);
 }

@@ -352,22 +352,45 @@ class Engine:
         # ---- spectra (xcorrnm2_tri zorro.py:814-925)
         bench["xcorr0"] = time.time()
         se = int(self.lib.zr_spectrum_elems(C0, C1))
-        G = self.tensor("G", (N, se, 2), torch.float32)
-        S = self.tensor("S", (N, se, 2), torch.float32)
-        GM = self.tensor("GM", (se, 2), torch.float32)
+        half = str(getattr(reg, "spectraPrecision", "float32")).lower() in ("float16", "half", "f16")
+        if half and reg.triMode == "refine":
+            raise ValueError("triMode 'refine' builds its templates from float32 spectra (spectraPrecision 'float32')")
         mrows = P0 if mask_dev is not None else H
         wbm = self.lib.zr_spectra_work_bytes(mrows, 1, C1)
-        self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None, None, 0, 1,
-                  1, P0, P1, C0, C1, GM.data_ptr(), None, self.ptr("specwork", wbm), wbm, st)
         per = self.lib.zr_spectra_work_bytes(H, 1, C1)
         chunk = max(1, min(N, SPECTRA_WORK // per))
+        if half:
+            # half-precision store with per-spectrum power-of-two scales: each
+            # chunk of frames goes through a float32 staging buffer, then packed
+            G16 = self.tensor("G16", (N, se), torch.int32)
+            S16 = self.tensor("S16", (N, se), torch.int32)
+            GM16 = self.tensor("GM16", (se,), torch.int32)
+            hsc = self.tensor("hscales", (2 * N + 1,), torch.float32)
+            pw = self.ptr("packwork", 4 * max(N, 1))
+            G = self.tensor("G", (chunk, se, 2), torch.float32)
+            S = self.tensor("S", (chunk, se, 2), torch.float32)
+        else:
+            G = self.tensor("G", (N, se, 2), torch.float32)
+            S = self.tensor("S", (N, se, 2), torch.float32)
+        GM = self.tensor("GM", (se, 2), torch.float32)
+        self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None, None, 0, 1,
+                  1, P0, P1, C0, C1, GM.data_ptr(), None, self.ptr("specwork", wbm), wbm, st)
+        if half:
+            self.call("C_spectra", "zr_pack_half", GM.data_ptr(), 1, se, GM16.data_ptr(), hsc[2 * N:].data_ptr(),
+                      pw, 4 * N, st)
         wb = per * chunk
         wptr = self.ptr("specwork", wb)
         for f0 in range(0, N, chunk):
             nf = min(chunk, N - f0)
+            g0 = 0 if half else f0
             self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None,
                       msub.data_ptr() if msub is not None else None, f0, nf, 0, P0, P1, C0, C1,
-                      G[f0].data_ptr(), S[f0].data_ptr(), wptr, wb, st)
+                      G[g0].data_ptr(), S[g0].data_ptr(), wptr, wb, st)
+            if half:
+                self.call("C_spectra", "zr_pack_half", G.data_ptr(), nf, se, G16[f0].data_ptr(), hsc[f0:].data_ptr(),
+                          pw, 4 * N, st)
+                self.call("C_spectra", "zr_pack_half", S.data_ptr(), nf, se, S16[f0].data_ptr(),
+                          hsc[N + f0:].data_ptr(), pw, 4 * N, st)
 
         # ---- correlation windows and peaks (mnxc2 / locatePeak)
         refine = reg.triMode == "refine"
@@ -381,8 +404,13 @@ class Engine:
         terms = self.tensor("terms", (4 * N + 1, w, w), torch.float32)
         xw = min(XCORR_WORK, max(self.lib.zr_xcorr_work_bytes(1, C1, mS), self.lib.zr_xcorr_work_bytes(M, C1, mS)))
         xptr = self.ptr("xcwork", xw)
-        self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), N, C0, C1, mS, terms.data_ptr(), xptr,
-                  xw, st)
+        if half:
+            # products, inverse transforms and the combination stay float32
+            self.call("D_frame_terms", "zr_xcorr_terms_half", G16.data_ptr(), S16.data_ptr(), GM16.data_ptr(),
+                      hsc.data_ptr(), N, C0, C1, mS, terms.data_ptr(), xptr, xw, st)
+        else:
+            self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), N, C0, C1, mS,
+                      terms.data_ptr(), xptr, xw, st)
         cwin = self.tensor("cwin", (max(M, 1), w, w), torch.float32)
         if refine:
             TG = self.tensor("refineT", (N, se, 2), torch.float32)
@@ -391,6 +419,10 @@ class Engine:
             self.call("E_pairs", "zr_refine_terms", terms.data_ptr(), N, mS, rterms.data_ptr(), st)
             self.call("E_pairs", "zr_xcorr_refine", G.data_ptr(), TG.data_ptr(), rterms.data_ptr(), N, C0, C1, mS,
                       cwin.data_ptr(), xptr, xw, st)
+        elif half:
+            pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
+            self.call("E_pairs", "zr_xcorr_pairs_half", G16.data_ptr(), hsc.data_ptr(), terms.data_ptr(),
+                      pairs_dev.data_ptr(), M, N, C0, C1, mS, cwin.data_ptr(), xptr, xw, st)
         else:
             pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
             self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pairs_dev.data_ptr(), M, N, C0, C1,

@@ -101,7 +101,30 @@ class ImageRegistrator:
         self.keepAlignedImages = True   # copy the shifted frames back into ``images``
         self.subtractFrameMean = True    # exact identity, see zorro_gb300.engine
         self.returnDeviceArrays = False  # leave imageSum/filtSum/FRC as CUDA tensors
+        # 'float16': frame spectra stored in half precision with per-spectrum
+        # power-of-two scales (products and transforms stay float32)
+        self.spectraPrecision = "float32"
         self.device = 0
+
+    def loadGainRef(self, gain):
+        """Set ``gainRef`` from a gain-reference array as loadData does when it
+        reads one (target 'gainRef', zorro.py:3486-3502): rotated by 90
+        degrees if gainInfo['Diagonal'], then rotated by 180 degrees if both
+        'Horizontal' and 'Vertical', else flipped left-right ('Horizontal')
+        or up-down ('Vertical').  The multiply by the frames (zorro.py:3466)
+        happens inside the kernels that read them."""
+        g = np.asarray(gain, dtype=np.float32)
+        info = self.gainInfo or {}
+        if info.get("Diagonal"):
+            g = np.rot90(g, k=1)
+        if info.get("Horizontal") and info.get("Vertical"):
+            g = np.rot90(g, k=2)
+        elif info.get("Horizontal"):
+            g = np.fliplr(g)
+        elif info.get("Vertical"):
+            g = np.flipud(g)
+        self.gainRef = np.ascontiguousarray(g)
+        return self.gainRef
 
     def alignImageStack(self):
         """Register and sum the stack.  zorro.py:1569-1716."""
