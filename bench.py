@@ -253,6 +253,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slots", type=int, default=2, help="movies in flight on the served path")
     ap.add_argument("--profile-only", action="store_true", help="run the warm-up and 2 steps, no timing output")
+    ap.add_argument("--no-poisson", action="store_true", help="skip the open-loop Poisson-arrival serving runs")
+    ap.add_argument("--poisson-seconds", type=float, default=3.0, help="arrival window per Poisson rate")
+    ap.add_argument("--no-fp16", action="store_true", help="skip the half-precision-spectra run")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -340,6 +343,29 @@ def main():
         t_step = float(tt.item())
     value = world / t_step
 
+    # ---- the same movies with half-precision frame spectra (spectraPrecision 'float16')
+    fp16 = None
+    Cc = int(wl["attrs"]["fouCrop"][0])
+    if not args.no_fp16:
+        def make_reg16():
+            r = make_reg(raw_dev, gain_dev, True)
+            r.spectraPrecision = "float16"
+            return r
+        for _ in range(2):
+            make_reg16().alignImageStack()
+        barrier()
+        h0 = torch.cuda.Event(enable_timing=True)
+        h1 = torch.cuda.Event(enable_timing=True)
+        h0.record()
+        for _ in range(args.steps):
+            make_reg16().alignImageStack()
+        h1.record()
+        barrier()
+        t16 = h0.elapsed_time(h1) / 1000.0 / args.steps
+        fp16 = {"value": round(world / t16, 3), "unit": UNIT, "ms_per_step": round(t16 * 1e3, 3),
+                "spectra_bytes_half": int(2 * N * (Cc // 2 + 1) * Cc * 4),
+                "spectra_bytes_float": int(2 * N * (Cc // 2 + 1) * Cc * 8)}
+
     # ---- served path: movies in flight in parallel slots (continuous batching)
     from zorro_gb300.serve import MovieServer
     srv = MovieServer(device=local, slots=args.slots, hbm_budget=160e9)
@@ -354,6 +380,26 @@ def main():
     barrier()
     t_served = (time.perf_counter() - sv0) / (args.steps * args.slots)
     served = srv.stats()
+    # open-loop serving: Poisson arrivals at fixed rates, latency = arrival to result
+    poisson = []
+    if not args.no_poisson:
+        rng = np.random.default_rng(7 + rank)
+        for rate in (2.0, 8.0, 32.0):
+            srv.reset_stats()
+            n_req = max(8, int(args.poisson_seconds * rate))
+            gaps = rng.exponential(1.0 / rate, size=n_req)
+            t_start = time.perf_counter()
+            futs = []
+            for g in gaps:
+                t_start += g
+                while time.perf_counter() < t_start:
+                    time.sleep(min(0.002, max(0.0, t_start - time.perf_counter())))
+                futs.append(srv.submit(make_reg(raw_dev, gain_dev, True)))
+            for f in futs:
+                f.result()
+            st_ = srv.stats()
+            poisson.append({"rate_per_s": rate, "requests": n_req, "movies_per_s": round(st_["movies_per_s"], 3),
+                            "p50_ms": round(st_["p50_s"] * 1e3, 2), "p99_ms": round(st_["p99_s"] * 1e3, 2)})
     srv.close()
     if dist is not None:
         tt = torch.tensor([t_served], device=dev)
@@ -426,7 +472,8 @@ def main():
                         "d2h_bytes_per_step": d2h},
                 "served": {"value": round(world / t_served, 3), "unit": UNIT, "slots": args.slots,
                            "p50_ms": round(served["p50_s"] * 1e3, 2), "p99_ms": round(served["p99_s"] * 1e3, 2),
-                           "vs_plain": round((world / t_served) / value, 3)},
+                           "vs_plain": round((world / t_served) / value, 3), "poisson": poisson},
+                "fp16_spectra": fp16,
                 "gpu_launches": int(launches),
                 "wall_s_timed": round(wall, 3),
                 "clocks": clk.summary(),
