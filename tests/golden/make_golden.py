@@ -46,6 +46,11 @@ CASES = {
     "evenodd_frc": dict(movie=dict(n_frames=40, shape=(800, 780), seed=21, mean_dose=1.5, drift_sigma=0.8),
                         attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[512, 512], maxShift=20,
                                    pixelsize=0.1, doEvenOddFRC=True)),
+    # a Fourier crop of 3 x 2^k (the reference's default crop is 3072) with the dose filter
+    "crop768": dict(movie=dict(n_frames=12, shape=(700, 650), seed=17, mean_dose=1.5, drift_sigma=1.0),
+                    attrs=dict(triMode="diag", diagWidth=4, shapePadded=[1024, 1024], fouCrop=[768, 768],
+                               maxShift=30, pixelsize=0.1, filterMode="dose", doseFiltParam=DOSE,
+                               doLazyFRC=False)),
     # refine mode: each frame against the sum of the others, no solver
     "refine_mode": dict(movie=dict(n_frames=10, shape=(200, 180), seed=12, mean_dose=1.5, drift_sigma=0.8),
                         attrs=dict(triMode="refine", shapePadded=[256, 256], fouCrop=[128, 128], maxShift=20,

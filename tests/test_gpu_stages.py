@@ -21,7 +21,8 @@ def crop_layout(F, P, C_):
     return F[np.array(rows)][:, :C1 // 2 + 1]
 
 
-@pytest.mark.parametrize("P,C_", [((128, 128), (64, 64)), ((128, 256), (128, 128)), ((256, 256), (256, 256))])
+@pytest.mark.parametrize("P,C_", [((128, 128), (64, 64)), ((128, 256), (128, 128)), ((256, 256), (256, 256)),
+                                  ((1536, 1536), (768, 384)), ((1536, 3072), (1536, 3072))])
 def test_spectra_match_numpy_fft(small, P, C_):
     from tests import gpu_helpers as gh
     G, S, GM, means, _ = gh.spectra(small, P, C_)
@@ -40,7 +41,8 @@ def test_spectra_match_numpy_fft(small, P, C_):
         np.testing.assert_allclose(S[n][:, :C_[1] // 2 + 1], s_ref, atol=2e-6 * np.abs(s_ref).max() * np.sqrt(P[0] * P[1]) / 16)
 
 
-@pytest.mark.parametrize("P,C_,mS", [((128, 128), (64, 64), 12), ((256, 256), (128, 128), 20)])
+@pytest.mark.parametrize("P,C_,mS", [((128, 128), (64, 64), 12), ((256, 256), (128, 128), 20),
+                                     ((1536, 1536), (768, 384), 20), ((3072, 3072), (1536, 1536), 24)])
 def test_correlation_windows_match_oracle(small, P, C_, mS):
     """C windows of mnxc2 (float32, mean-subtracted) vs the float64 oracle."""
     from tests import gpu_helpers as gh

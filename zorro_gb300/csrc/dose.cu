@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(fft_threads(P1, DS_NBR), fft_minblocks(P1))
     float2 U = make_float2(0.0f, 0.0f), V = U;
     if (k <= P1 / 2) {
       const float2 zk = sm[r * LD + pidx(k)];
-      const float2 zm = sm[r * LD + pidx((P1 - k) & (P1 - 1))];
+      const float2 zm = sm[r * LD + pidx(k == 0 ? 0 : P1 - k)];
       U = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
       V = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
     }
@@ -252,7 +252,9 @@ static int set_smem(const void* fn, size_t smem) {
     case 256: { constexpr int LL = 256; CALL; } break;          \
     case 512: { constexpr int LL = 512; CALL; } break;          \
     case 1024: { constexpr int LL = 1024; CALL; } break;        \
+    case 1536: { constexpr int LL = 1536; CALL; } break;        \
     case 2048: { constexpr int LL = 2048; CALL; } break;        \
+    case 3072: { constexpr int LL = 3072; CALL; } break;        \
     case 4096: { constexpr int LL = 4096; CALL; } break;        \
     default: return set_error(ZR_ESIZE, "dose filter size %d not supported", (int)(L)); \
   }
@@ -315,8 +317,9 @@ extern "C" int zr_dose_filter(const float* aligned, int N, int H, int W, const z
   if (!aligned || !params || !thres_q || !dose_end || !filt_sum || !work)
     return set_error(ZR_EINVAL, "zr_dose_filter: null argument");
   if (N <= 0 || H <= 0 || W <= 0 || H > P0 || W > P1) return set_error(ZR_EINVAL, "zr_dose_filter: bad sizes");
-  if (!is_pow2(P0) || !is_pow2(P1) || P0 < 256 || P1 < 256 || P0 > 4096 || P1 > 4096)
-    return set_error(ZR_ESIZE, "zr_dose_filter: padded size %dx%d must be a power of two in [256, 4096]", P0, P1);
+  if (!fft_len_ok(P0) || !fft_len_ok(P1) || P0 < 256 || P1 < 256 || P0 > 4096 || P1 > 4096)
+    return set_error(ZR_ESIZE, "zr_dose_filter: padded size %dx%d must be a power of two in [256, 4096], 1536 or 3072",
+                     P0, P1);
   const size_t fixed = dose_fixed_bytes(P0, P1), per = dose_frame_bytes(P0, P1);
   if (work_bytes < fixed + 2 * per)
     return set_error(ZR_EWORK, "zr_dose_filter: work buffer %zu < %zu", work_bytes, fixed + 2 * per);

@@ -1,17 +1,19 @@
 // Batched complex FFTs held in shared memory, for sm_103a.
 //
-// A CTA transforms NB sequences of length L (a power of two, 2..8192) that sit
-// in shared memory.  Element i of sequence b lives at s[b*ld(L) + pidx(i)]:
+// A CTA transforms NB sequences of length L (L = 2^a 3^b 5^c dividing TWN,
+// e.g. 64..4096 and 3 x 2^k) that sit in shared memory.  Element i of sequence b lives at s[b*ld(L) + pidx(i)]:
 // one padding slot every 16 elements keeps the radix-16 scatter of the first
 // pass free of bank conflicts, and the row pitch (ld_of) keeps tiles of 4
 // sequences x 4 elements conflict-free.  Each pass is a radix-16 Stockham
 // step (the last pass radix 2, 4 or 8 when log2(L) is not a multiple of 4):
 // every thread reads its butterflies' inputs into registers, the CTA
 // synchronises, and the outputs are written back in place.  No ping-pong
-// buffer is needed.
+// buffer is needed.  Lengths with a factor 3 or 5 end with radix-3 / radix-5
+// passes.
 //
-// Twiddles come from a table of W_8192^k = exp(-2 pi i k / 8192) computed in
-// double precision on the host and rounded to float (``tw`` argument).
+// Twiddles come from a table of W_TWN^k = exp(-2 pi i k / TWN), TWN = 2^12 x
+// 3 x 5, computed in double precision on the host and rounded to float
+// (``tw`` argument); a length-L transform reads every (TWN/L)-th entry.
 // DIR = -1 is the forward transform, +1 the inverse; neither is normalised.
 #pragma once
 #include <cuda_runtime.h>
@@ -19,7 +21,7 @@
 
 namespace zr {
 
-constexpr int TWN = 8192;  // twiddle table length
+constexpr int TWN = 61440;  // twiddle table length: 2^12 * 3 * 5
 
 __host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 4); }
 // Row pitch of one sequence: the padded length rounded so that pitch = 4
@@ -128,11 +130,58 @@ __device__ __forceinline__ void dft<16, -1>(float2* x) { dft16<-1>(x); }
 template <>
 __device__ __forceinline__ void dft<16, 1>(float2* x) { dft16<1>(x); }
 
+// 3-point DFT: X1,2 = a - (b + c)/2 +/- DIR i sin(2 pi/3) (b - c)
+template <int DIR>
+__device__ __forceinline__ void dft3(float2* x) {
+  const float s = 0.86602540378443864676f;
+  const float2 a = x[0], b = x[1], c = x[2];
+  const float2 bc = cadd(b, c);
+  const float2 t = make_float2(a.x - 0.5f * bc.x, a.y - 0.5f * bc.y);
+  const float2 d = csub(b, c);
+  const float2 u = mul_si<DIR>(make_float2(s * d.x, s * d.y));
+  x[0] = cadd(a, bc);
+  x[1] = cadd(t, u);
+  x[2] = csub(t, u);
+}
+template <>
+__device__ __forceinline__ void dft<3, -1>(float2* x) { dft3<-1>(x); }
+template <>
+__device__ __forceinline__ void dft<3, 1>(float2* x) { dft3<1>(x); }
+
+// 5-point DFT with the pairs (1,4) and (2,3): cos/sin of 2 pi/5 and 4 pi/5
+template <int DIR>
+__device__ __forceinline__ void dft5(float2* x) {
+  const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
+  const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;
+  const float2 b1 = cadd(x[1], x[4]), b2 = cadd(x[2], x[3]);
+  const float2 d1 = csub(x[1], x[4]), d2 = csub(x[2], x[3]);
+  const float2 a = x[0];
+  const float2 t1 = make_float2(a.x + c1 * b1.x + c2 * b2.x, a.y + c1 * b1.y + c2 * b2.y);
+  const float2 t2 = make_float2(a.x + c2 * b1.x + c1 * b2.x, a.y + c2 * b1.y + c1 * b2.y);
+  const float2 u1 = mul_si<DIR>(make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y));
+  const float2 u2 = mul_si<DIR>(make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y));
+  x[0] = make_float2(a.x + b1.x + b2.x, a.y + b1.y + b2.y);
+  x[1] = cadd(t1, u1);
+  x[4] = csub(t1, u1);
+  x[2] = cadd(t2, u2);
+  x[3] = csub(t2, u2);
+}
+template <>
+__device__ __forceinline__ void dft<5, -1>(float2* x) { dft5<-1>(x); }
+template <>
+__device__ __forceinline__ void dft<5, 1>(float2* x) { dft5<1>(x); }
+
+// Radix of the pass that starts after NS: 16 while it divides what is left,
+// then 8, 4, 2, then the odd factors 3 and 5.
+constexpr int fft_radix(int rem) {
+  return rem % 16 == 0 ? 16 : (rem % 8 == 0 ? 8 : (rem % 4 == 0 ? 4 : (rem % 2 == 0 ? 2 : (rem % 3 == 0 ? 3 : 5))));
+}
+
 // One Stockham pass (radix R, NS = product of the radices already applied),
 // then the remaining passes.
 template <int L, int NB, int T, int DIR, int NS>
 __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ tw) {
-  constexpr int R = (L / NS >= 16) ? 16 : (L / NS);
+  constexpr int R = fft_radix(L / NS);
   constexpr int LR = L / R;
   constexpr int NBF = NB * LR;
   constexpr int K = (NBF + T - 1) / T;
@@ -145,7 +194,7 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
     if ((NBF % T) == 0 || bf < NBF) {
       const int b = bf / LR, j = bf - (bf / LR) * LR;
       const float2* src = s + b * LD;
-      const int k = j & (NS - 1);
+      const int k = j % NS;
 #pragma unroll
       for (int r = 0; r < R; r++) v[i][r] = src[pidx(j + r * LR)];
       if (NS > 1) {
@@ -159,6 +208,10 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
         const float2 w1 = __ldg(tw + k * TWS);
         if constexpr (R == 2) {
           twiddle(1, w1);
+        } else if constexpr (R == 3 || R == 5) {
+          twiddle(1, w1);
+#pragma unroll
+          for (int r = 2; r < R; r++) twiddle(r, __ldg(tw + r * k * TWS));
         } else {
           const float2 w2 = __ldg(tw + 2 * k * TWS);
           const float2 w3 = (R == 16) ? __ldg(tw + 3 * k * TWS) : cmul(w1, w2);
@@ -185,7 +238,7 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
     if ((NBF % T) == 0 || bf < NBF) {
       const int b = bf / LR, j = bf - (bf / LR) * LR;
       float2* dst = s + b * LD;
-      const int k = j & (NS - 1);
+      const int k = j % NS;
       const int base = (j / NS) * NS * R + k;
 #pragma unroll
       for (int r = 0; r < R; r++) dst[pidx(base + r * NS)] = v[i][r];
@@ -200,7 +253,7 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
 // before (after filling ``s``); the function ends with a barrier.
 template <int L, int NB, int T, int DIR>
 __device__ __forceinline__ void block_fft(float2* s, const float2* __restrict__ tw) {
-  static_assert((L & (L - 1)) == 0 && L >= 2 && L <= TWN, "L must be a power of two <= 8192");
+  static_assert(L >= 2 && TWN % L == 0, "L must divide the twiddle table length 2^12 * 3 * 5");
   fft_pass<L, NB, T, DIR, 1>(s, tw);
 }
 

@@ -14,6 +14,9 @@ int launched(const char* what);
 const float2* twiddles();
 
 inline bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
+// Transform lengths the library is built for: powers of two and 3 x 2^k
+// (the reference's default Fourier crop is 3072).
+inline bool fft_len_ok(long long v) { return is_pow2(v) || v == 384 || v == 768 || v == 1536 || v == 3072; }
 inline int ilog2(long long v) {
   int l = 0;
   while ((1LL << l) < v) ++l;

@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
     float2 U = make_float2(0.0f, 0.0f), V = U;
     if (k <= half) {
       const float2 zk = sm[r * LD + pidx(k)];
-      const float2 zm = sm[r * LD + pidx((P1 - k) & (P1 - 1))];
+      const float2 zm = sm[r * LD + pidx(k == 0 ? 0 : P1 - k)];
       U = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
       V = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
     }
@@ -228,9 +228,11 @@ static int launch_cols(const float2* RU, const float2* RV, int rows, int C0, int
     case 256: { constexpr int LL = 256; CALL; } break;   \
     case 512: { constexpr int LL = 512; CALL; } break;   \
     case 1024: { constexpr int LL = 1024; CALL; } break; \
+    case 1536: { constexpr int LL = 1536; CALL; } break; \
     case 2048: { constexpr int LL = 2048; CALL; } break; \
+    case 3072: { constexpr int LL = 3072; CALL; } break; \
     case 4096: { constexpr int LL = 4096; CALL; } break; \
-    default: return set_error(ZR_ESIZE, "transform length %d not supported (powers of two 64..4096)", (int)(L)); \
+    default: return set_error(ZR_ESIZE, "transform length %d not supported (powers of two 64..4096, 1536, 3072)", (int)(L)); \
   }
 
 }  // namespace zr
@@ -262,8 +264,10 @@ extern "C" int zr_spectra(const zr_frames_t* frames, const float* mask, const do
                           size_t work_bytes, void* stream) {
   if (!frames || !G || (mode == 0 && (!S || !frames->raw)))
     return set_error(ZR_EINVAL, "zr_spectra: null argument");
-  if (!is_pow2(P0) || !is_pow2(P1) || !is_pow2(C0) || !is_pow2(C1) || C0 > P0 || C1 > P1 || C0 < 64 || C1 < 64)
-    return set_error(ZR_ESIZE, "zr_spectra: P=%dx%d C=%dx%d must be powers of two with 64 <= C <= P <= 4096", P0,
+  if (!fft_len_ok(P0) || !fft_len_ok(P1) || !fft_len_ok(C0) || !fft_len_ok(C1) || C0 > P0 || C1 > P1 || C0 < 64 ||
+      C1 < 64)
+    return set_error(ZR_ESIZE,
+                     "zr_spectra: P=%dx%d C=%dx%d must be powers of two or 3 x 2^k with 64 <= C <= P <= 4096", P0,
                      P1, C0, C1);
   FrameSrc f = make_src(frames);
   if (f.H > P0 || f.W > P1) return set_error(ZR_EINVAL, "zr_spectra: frame %dx%d larger than padded %dx%d", f.H, f.W, P0, P1);

@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks
   float2* out = Tw + (size_t)jl * rows * K4;
   for (int e = threadIdx.x; e < rows * XC_NBC; e += T) {
     const int a = e / XC_NBC, c = e - a * XC_NBC;
-    const int y = (a - mS) & (C0 - 1);
+    const int y = a < mS ? a - mS + C0 : a - mS;
     out[(size_t)a * K4 + k0 + c] = sm[c * LD + pidx(y)];
   }
 }
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
     const int p = q >> 1;
     const int a = arow0 + q;
     if (a >= rows) continue;
-    const int x = (b - mS) & (C1 - 1);
+    const int x = b < mS ? b - mS + C1 : b - mS;
     const float2 yv = sm[p * LD + pidx(x)];
     const float v = ((q & 1) ? yv.y : yv.x) * scale;
     const size_t pix = (size_t)a * w + b;
@@ -267,8 +267,12 @@ static int launch_xc_rows(const XcJobs& J, int nj, int C0, int K4, int mS, float
     case 128: { constexpr int LL = 128; CALL; } break;        \
     case 256: { constexpr int LL = 256; CALL; } break;        \
     case 512: { constexpr int LL = 512; CALL; } break;        \
+    case 384: { constexpr int LL = 384; CALL; } break;        \
+    case 768: { constexpr int LL = 768; CALL; } break;        \
     case 1024: { constexpr int LL = 1024; CALL; } break;      \
+    case 1536: { constexpr int LL = 1536; CALL; } break;      \
     case 2048: { constexpr int LL = 2048; CALL; } break;      \
+    case 3072: { constexpr int LL = 3072; CALL; } break;      \
     case 4096: { constexpr int LL = 4096; CALL; } break;      \
     default: return set_error(ZR_ESIZE, "crop size %d not supported", (int)(L)); \
   }
@@ -296,8 +300,8 @@ static int run_jobs(XcJobs J, int njobs, int C0, int C1, int mS, const float* te
 }
 
 static int check_sizes(int C0, int C1, int mS) {
-  if (!is_pow2(C0) || !is_pow2(C1) || C0 < 64 || C1 < 64 || C0 > 4096 || C1 > 4096)
-    return set_error(ZR_ESIZE, "crop %dx%d must be powers of two in [64, 4096]", C0, C1);
+  if (!fft_len_ok(C0) || !fft_len_ok(C1) || C0 < 64 || C1 < 64 || C0 > 4096 || C1 > 4096)
+    return set_error(ZR_ESIZE, "crop %dx%d must be powers of two in [64, 4096] or 3 x 2^k in [384, 3072]", C0, C1);
   if (mS < 2 || 2 * mS > C0 || 2 * mS > C1 || mS > 112)
     return set_error(ZR_ESIZE, "maxShift %d must satisfy 2 <= maxShift <= min(112, C/2)", mS);
   return ZR_OK;

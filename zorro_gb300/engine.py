@@ -41,6 +41,17 @@ XCORR_WORK = 256 << 20
 DOSE_WORK = 1536 << 20
 
 
+def _crop_ok(v):
+    return (_pow2(v) and 64 <= v <= 4096) or v in (384, 768, 1536, 3072)
+
+
+def _padded_ok(v):
+    return (_pow2(v) and 64 <= v <= 4096) or v in (1536, 3072)
+
+
+_CROP_OK, _PADDED_OK = _crop_ok, _padded_ok
+
+
 def _pow2(v):
     return v > 0 and (v & (v - 1)) == 0
 
@@ -323,9 +334,11 @@ class Engine:
             C0, C1 = (int(v) for v in 2 * np.floor(np.array(reg.fouCrop) / 2.0).astype(int))
         else:
             C0, C1 = P0, P1
-        for v, nm in ((P0, "shapePadded"), (P1, "shapePadded"), (C0, "fouCrop"), (C1, "fouCrop")):
-            if not _pow2(v):
-                raise ValueError("%s %d: the GPU path needs powers of two" % (nm, v))
+        for v, nm, ok in ((P0, "shapePadded", _PADDED_OK), (P1, "shapePadded", _PADDED_OK), (C0, "fouCrop", _CROP_OK),
+                          (C1, "fouCrop", _CROP_OK)):
+            if not ok(v):
+                raise ValueError("%s %d: the GPU path transforms powers of two (64..4096) and 1536, 3072 (padded) or "
+                                 "384, 768, 1536, 3072 (crop)" % (nm, v))
         mS = int(reg.maxShift)
         w = 2 * mS
         mask_dev = None
