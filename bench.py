@@ -98,6 +98,17 @@ def read_traffic():
     return out
 
 
+def slowest_rank(t_local, dist=None, device="cpu"):
+    """Seconds per step of the job: the maximum over ranks of each rank's
+    own time (each rank registers its own movies; no data-path collective)."""
+    if dist is None:
+        return float(t_local)
+    import torch
+    tt = torch.tensor([float(t_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -337,10 +348,7 @@ def main():
     if args.profile_only:
         return
     t_step = max(dev_ms / 1000.0, 1e-9) / args.steps
-    if dist is not None:
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = slowest_rank(t_step, dist, dev)
     value = world / t_step
 
     # ---- the same movies with half-precision frame spectra (spectraPrecision 'float16')
@@ -361,7 +369,7 @@ def main():
             make_reg16().alignImageStack()
         h1.record()
         barrier()
-        t16 = h0.elapsed_time(h1) / 1000.0 / args.steps
+        t16 = slowest_rank(h0.elapsed_time(h1) / 1000.0 / args.steps, dist, dev)
         fp16 = {"value": round(world / t16, 3), "unit": UNIT, "ms_per_step": round(t16 * 1e3, 3),
                 "spectra_bytes_half": int(2 * N * (Cc // 2 + 1) * Cc * 4),
                 "spectra_bytes_float": int(2 * N * (Cc // 2 + 1) * Cc * 8)}
@@ -401,10 +409,7 @@ def main():
             poisson.append({"rate_per_s": rate, "requests": n_req, "movies_per_s": round(st_["movies_per_s"], 3),
                             "p50_ms": round(st_["p50_s"] * 1e3, 2), "p99_ms": round(st_["p99_s"] * 1e3, 2)})
     srv.close()
-    if dist is not None:
-        tt = torch.tensor([t_served], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_served = float(tt.item())
+    t_served = slowest_rank(t_served, dist, dev)
 
     # ---- end to end through the public API from pinned host memory
     barrier()
@@ -418,10 +423,7 @@ def main():
     e1.record()
     barrier()
     t_e2e = e0.elapsed_time(e1) / 1000.0 / args.steps
-    if dist is not None:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = slowest_rank(t_e2e, dist, dev)
     h2d = raw_np.nbytes + (gain_np.nbytes if gain_np is not None else 0)
     d2h = 4 * H * W * 2 + 512 * 512 * 4 + 256 * 8 + N * 2 * 8
 
