@@ -141,6 +141,17 @@ int zr_hotpix_maps(const float* unaligned_sum, int height, int width, int n_fram
                    const zr_hotpix_params_t* params, float* hot_a, float* hot_b,
                    unsigned int* counts3, void* work, size_t work_bytes, void* stream);
 
+/* ---- Fourier binning: binStack(binKernel='fourier'), zorro.py:1826-1904 ----
+ * out[n] (float, [Hb][Wb]) = real(IFFT_unscaled(crop(FFT(frame n))) / (Hb Wb)),
+ * the crop keeping rows [0, Hb/2) and [H - Hb/2, H) and columns likewise; the
+ * frames are read with their gain (hot-pixel maps are not applied: the
+ * reference bins before its hot-pixel filter).  Hb and Wb even; every side
+ * in 513..8192 (Bluestein transforms of 2048..16384 points).  work:
+ * zr_bin_work_bytes(H, W, Hb, Wb) bytes. */
+size_t zr_bin_work_bytes(int H, int W, int Hb, int Wb);
+int zr_bin_fourier(const zr_frames_t* frames, int Hb, int Wb, float* out, void* work, size_t work_bytes,
+                   void* stream);
+
 /* ---- forward spectra: xcorrnm2_tri, zorro.py:814-925 ---- */
 
 /* sums[n] (double, accumulated) += sum of the corrected frame n over

@@ -70,6 +70,25 @@ def tri_indices(N, triMode="diag", diagWidth=5, diagStart=0):
     return trimesh >= 1
 
 
+def bin_stack(images, shapeBinned, dt):
+    """Fourier binning, binStack(binKernel='fourier').  zorro.py:1826-1904:
+    per frame the full FFT, the four corners of Hb/2 x Wb/2 kept, times
+    1/(Hb Wb), the unscaled inverse, its real part as float32."""
+    b0, b1 = int(shapeBinned[0]) // 2, int(shapeBinned[1]) // 2
+    out = np.zeros([images.shape[0], int(shapeBinned[0]), int(shapeBinned[1])], dtype="float32")
+    normConst = 1.0 / (shapeBinned[0] * shapeBinned[1])
+    for J in range(images.shape[0]):
+        F = dt.fft2(images[J].astype(dt.c))
+        B = np.zeros([int(shapeBinned[0]), int(shapeBinned[1])], dtype=dt.c)
+        B[:b0, :b1] = F[:b0, :b1]
+        B[:b0, -b1:] = F[:b0, -b1:]
+        B[-b0:, :b1] = F[-b0:, :b1]
+        B[-b0:, -b1:] = F[-b0:, -b1:]
+        B *= normConst
+        out[J] = np.real(dt.ifft2(B))
+    return out
+
+
 def pad_stack(images, shapePadded):
     """Zero-pad at the top-left and build the [1,P,P] mask.  zorro.py:1908-1958."""
     m, H, W = images.shape
@@ -743,7 +762,7 @@ def hotpix_filter(images, hotpixInfo, neighbourThres=0.01, dt=None):
 # the whole call
 # --------------------------------------------------------------------------
 
-DEFAULTS = dict(shapePadded=[4096, 4096], fouCrop=[3072, 3072], triMode="diag", diagWidth=5, diagStart=0,
+DEFAULTS = dict(shapeBinned=None, shapePadded=[4096, 4096], fouCrop=[3072, 3072], triMode="diag", diagWidth=5, diagStart=0,
                 maxShift=100, subPixReg=16, Bmode="opti", Brad=512, weightMode="autologistic",
                 peaksigThres=6.0, logisticK=5.0, logisticNu=0.15, originMode="centroid",
                 suppressOrigin=True, shiftMethod="lanczos", doLazyFRC=True, doEvenOddFRC=False, filterMode=None,
@@ -795,6 +814,13 @@ def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
     images = np.array(images, copy=True)
     res = {}
     fm = (o["filterMode"] or "").lower()
+    if o.get("shapeBinned") is not None and np.any(o["shapeBinned"]):
+        # zorro.py:1588-1589 and 1834-1836: binned first, pixel size scaled
+        scale = np.array(images.shape[1:]) / np.array(o["shapeBinned"])
+        if o["pixelsize"] is not None:
+            o["pixelsize"] = o["pixelsize"] * np.mean(scale)
+        images = bin_stack(images, o["shapeBinned"], dt)
+        res["pixelsize"] = o["pixelsize"]
     if "hot" in fm:
         bench["hot0"] = time.time()
         images, info, _ = hotpix_filter(images, o["hotpixInfo"], dt=dt)

@@ -51,6 +51,11 @@ CASES = {
                     attrs=dict(triMode="diag", diagWidth=4, shapePadded=[1024, 1024], fouCrop=[768, 768],
                                maxShift=30, pixelsize=0.1, filterMode="dose", doseFiltParam=DOSE,
                                doLazyFRC=False)),
+    # Fourier binning (binStack) of 1400 x 1300 frames to 700 x 650, then the usual path
+    "bin_fourier": dict(movie=dict(n_frames=12, shape=(1400, 1300), seed=19, mean_dose=0.5, drift_sigma=1.5),
+                        attrs=dict(triMode="tri", shapeBinned=[700, 650], shapePadded=[1024, 1024],
+                                   fouCrop=[512, 512], maxShift=30, pixelsize=0.05, filterMode="dose",
+                                   doseFiltParam=DOSE)),
     # refine mode: each frame against the sum of the others, no solver
     "refine_mode": dict(movie=dict(n_frames=10, shape=(200, 180), seed=12, mean_dose=1.5, drift_sigma=0.8),
                         attrs=dict(triMode="refine", shapePadded=[256, 256], fouCrop=[128, 128], maxShift=20,

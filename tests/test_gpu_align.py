@@ -293,3 +293,16 @@ def test_half_precision_spectra(name):
     assert rmse <= 0.05
     assert np.abs(reg.translations - ref["translations"]).max() <= 0.25
     assert rel_l2(reg.imageSum, ref["imageSum"]) <= 2e-2
+
+
+def test_binned_movie_against_oracle():
+    """shapeBinned: the movie Fourier-binned 2x on the GPU, then registered."""
+    mv = make_movie(n_frames=20, shape=(1400, 1300), seed=23, mean_dose=0.5, drift_sigma=1.2)
+    attrs = dict(triMode="tri", shapeBinned=[700, 650], shapePadded=[1024, 1024], fouCrop=[512, 512], maxShift=30,
+                 pixelsize=0.05, filterMode="dose", doseFiltParam=DOSE)
+    reg = gpu_align(mv["images"].copy(), **attrs)
+    ref = zo.align_image_stack(mv["images"], **attrs)
+    assert reg.pixelsize == pytest.approx(ref["pixelsize"])
+    assert np.abs(reg.translations - ref["translations"]).max() <= TRAJ_TOL
+    assert rel_l2(reg.imageSum, ref["imageSum"]) <= SUM_TOL
+    assert rel_l2(reg.filtSum, ref["filtSum"]) <= SUM_TOL

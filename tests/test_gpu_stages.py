@@ -90,3 +90,27 @@ def test_peaks_match_oracle_on_same_windows(small):
         if not same:
             assert np.abs(np.array([res["sy"][k], res["sx"][k]]) - r["shift"]).max() <= 1.0 / 16 + 1e-9
     assert agree >= len(pairs) - 1
+
+
+@pytest.mark.parametrize("shape,binned", [((1400, 1300), (700, 650)), ((1100, 1030), (540, 520))])
+def test_fourier_binning_matches_oracle(shape, binned):
+    """zr_bin_fourier (Bluestein transforms of any length) against the
+    float64 oracle's binStack."""
+    import ctypes as C
+    from tests import gpu_helpers as gh
+    from zorro_gb300 import _lib
+    torch = gh.torch_mod()
+    lib = _lib.load()
+    _lib.call("zr_init", torch.cuda.current_device())
+    mv = make_movie(3, shape, seed=5, mean_dose=1.0, drift_sigma=1.0)
+    raw = gh.dev_tensor(mv["images"].astype(np.float32))
+    fr = gh.frames_of(raw)
+    wb = lib.zr_bin_work_bytes(shape[0], shape[1], binned[0], binned[1])
+    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+    out = torch.zeros((3, binned[0], binned[1]), dtype=torch.float32, device="cuda")
+    _lib.call("zr_bin_fourier", C.byref(fr), binned[0], binned[1], out.data_ptr(), work.data_ptr(), wb, gh.stream())
+    torch.cuda.synchronize()
+    ref = zo.bin_stack(mv["images"].astype(np.float32), binned, zo.Dtypes(True))
+    got = out.cpu().numpy()
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < 2e-5, err

@@ -273,12 +273,24 @@ class Engine:
             # that shift method needs (self.__sC2 is undefined, zorro.py:891-895)
             raise AttributeError("shiftMethod 'fourier' is broken in the reference: self.__sC2 is undefined "
                                  "(zorro.py:895)")
-        if reg.shapeBinned is not None and np.any(reg.shapeBinned):
-            raise ValueError("shapeBinned (Fourier binning) is not supported by the GPU path yet")
         raw, gain, rtype = self.upload(reg)
         N, H, W = (int(s) for s in raw.shape)
         gdiv = float(reg.gain) if (reg.gain and not np.isclose(reg.gain, 1.0) and rtype != _lib.ZR_F32) else 0.0
         frames = self._frames(raw, rtype, gain, gdiv=gdiv)
+        pixelsize = reg.pixelsize
+        if reg.shapeBinned is not None and np.any(reg.shapeBinned):
+            # binStack (zorro.py:1826-1904), before the hot-pixel filter as there
+            Hb, Wb = int(reg.shapeBinned[0]), int(reg.shapeBinned[1])
+            bwb = self.lib.zr_bin_work_bytes(H, W, Hb, Wb)
+            binned = self.tensor("binned", (N, Hb, Wb), torch.float32)
+            self.call("A_gain_sum", "zr_bin_fourier", C.byref(frames), Hb, Wb, binned.data_ptr(),
+                      self.ptr("binwork", bwb), bwb, st)
+            scale = np.array([H, W], dtype=np.float64) / np.array([Hb, Wb], dtype=np.float64)
+            if pixelsize is not None:
+                pixelsize = pixelsize * np.mean(scale)
+            raw, gain, rtype, gdiv = binned, None, _lib.ZR_F32, 0.0
+            N, H, W = (int(v) for v in binned.shape)
+            frames = self._frames(raw, rtype, gain)
         hotinfo = dict(reg.hotpixInfo)
         filt = [f for f in (reg.filterMode or "").lower().replace(" ", "").split(",") if f]
 
@@ -572,7 +584,7 @@ class Engine:
         for fm in filt:
             if fm in ("dose", "dosenorm"):
                 mean_sum = float(isum.double().mean().item()) if reg.doseFiltParam[0] is None else None
-                dc = hm.dose_constants(N, [P0, P1], reg.pixelsize, reg.voltage, reg.doseFiltParam, mean_sum)
+                dc = hm.dose_constants(N, [P0, P1], pixelsize, reg.voltage, reg.doseFiltParam, mean_sum)
                 dp = DoseParams(dc["A"], dc["B"], dc["C"], dc["order"], dc["vs"], dc["invPSx"], dc["invPSy"],
                                 int(fm == "dosenorm"))
                 tq = torch.from_numpy(dc["thresQ"].astype(np.float32)).to(self.dev, non_blocking=True)
@@ -620,6 +632,7 @@ class Engine:
                     out[k] = out[k].numpy()
         out["hotpixInfo"] = hotinfo
         out["shapeOriginal"] = [H, W]
+        out["pixelsize"] = pixelsize
         out["masks"] = np.ones([1, H, W], dtype=bool) if not user_mask else reg.masks
         bench["align1"] = time.time()
         b = dict(reg.bench)
