@@ -36,39 +36,16 @@ __global__ void __launch_bounds__(fft_threads(P1, DS_NBR), fft_minblocks(P1))
   const int g = blockIdx.x;
   const int pl = blockIdx.y;              // frame pair within the chunk
   const int na = f0 + 2 * pl, nb = na + 1;
-  // DR_UNR pixels per thread are loaded before any is stored, so that several
-  // loads per thread are in flight
-  constexpr int NE = DS_NBR * P1;
-  constexpr int DR_UNR = 4;
   const float* ia = img + (size_t)na * H * W;
   const float* ib = img + (size_t)(nb < N ? nb : na) * H * W;
-  for (int e0 = threadIdx.x; e0 < NE; e0 += T * DR_UNR) {
-    float av[DR_UNR], bv[DR_UNR];
-#pragma unroll
-    for (int u = 0; u < DR_UNR; u++) {
-      const int e = e0 + u * T;
-      av[u] = bv[u] = 0.0f;
-      if (e < NE) {
-        const int r = e / P1, x = e - r * P1;
-        const int yy = g * DS_NBR + r;
-        const int ys = yy < H ? yy : (yy < 2 * H ? 2 * H - 1 - yy : sym_idx(yy, H));
-        const int xs = x < W ? x : (x < 2 * W ? 2 * W - 1 - x : sym_idx(x, W));
-        const size_t p = (size_t)ys * W + xs;
-        av[u] = __ldg(ia + p);
-        if (nb < N) bv[u] = __ldg(ib + p);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < DR_UNR; u++) {
-      const int e = e0 + u * T;
-      if (e < NE) {
-        const int r = e / P1, x = e - r * P1;
-        sm[r * LD + pidx(x)] = make_float2(av[u], bv[u]);
-      }
-    }
-  }
-  __syncthreads();
-  block_fft<P1, DS_NBR, T, -1>(sm, tw);
+  // element x of row r: the symmetric padding of the two frames' row
+  block_fft_from<P1, DS_NBR, T, -1>(sm, tw, [&](int r, int x) {
+    const int yy = g * DS_NBR + r;
+    const int ys = yy < H ? yy : (yy < 2 * H ? 2 * H - 1 - yy : sym_idx(yy, H));
+    const int xs = x < W ? x : (x < 2 * W ? 2 * W - 1 - x : sym_idx(x, W));
+    const size_t p = (size_t)ys * W + xs;
+    return make_float2(__ldg(ia + p), nb < N ? __ldg(ib + p) : 0.0f);
+  });
   // output: column-major per frame, [frame][kx][ky]
   const size_t fa = (size_t)(2 * pl) * K4 * P0;
   const size_t fb = fa + (size_t)K4 * P0;

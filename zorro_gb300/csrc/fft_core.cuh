@@ -177,6 +177,39 @@ constexpr int fft_radix(int rem) {
   return rem % 16 == 0 ? 16 : (rem % 8 == 0 ? 8 : (rem % 4 == 0 ? 4 : (rem % 2 == 0 ? 2 : (rem % 3 == 0 ? 3 : 5))));
 }
 
+// v[r] *= W^(k r) for r = 1 .. R-1 (W = exp(DIR 2 pi i / (TWN / TWS))): a
+// few powers from the table, the others as products of two table values (one
+// extra rounding), which keeps the load/store pipe for the data.
+template <int R, int DIR, int TWS>
+__device__ __forceinline__ void apply_twiddles(float2* v, int k, const float2* __restrict__ tw) {
+  auto twiddle = [&](int r, float2 ww) {
+    if (DIR > 0) ww.y = -ww.y;
+    v[r] = cmul(v[r], ww);
+  };
+  const float2 w1 = __ldg(tw + k * TWS);
+  if constexpr (R == 2) {
+    twiddle(1, w1);
+  } else if constexpr (R == 3 || R == 5) {
+    twiddle(1, w1);
+#pragma unroll
+    for (int r = 2; r < R; r++) twiddle(r, __ldg(tw + r * k * TWS));
+  } else {
+    const float2 w2 = __ldg(tw + 2 * k * TWS);
+    const float2 w3 = (R == 16) ? __ldg(tw + 3 * k * TWS) : cmul(w1, w2);
+    twiddle(1, w1);
+    twiddle(2, w2);
+    twiddle(3, w3);
+#pragma unroll
+    for (int a = 4; a < R; a += 4) {
+      const float2 wa = __ldg(tw + a * k * TWS);
+      twiddle(a, wa);
+      twiddle(a + 1, cmul(R == 16 ? wa : w1, R == 16 ? w1 : wa));
+      twiddle(a + 2, cmul(w2, wa));
+      twiddle(a + 3, cmul(w3, wa));
+    }
+  }
+}
+
 // One Stockham pass (radix R, NS = product of the radices already applied),
 // then the remaining passes.
 template <int L, int NB, int T, int DIR, int NS>
@@ -197,37 +230,7 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
       const int k = j % NS;
 #pragma unroll
       for (int r = 0; r < R; r++) v[i][r] = src[pidx(j + r * LR)];
-      if (NS > 1) {
-        // W^(k r) for r = 1 .. R-1: a few powers from the table, the others
-        // as products of two table values (one extra rounding), which keeps
-        // the load/store pipe for the data
-        auto twiddle = [&](int r, float2 ww) {
-          if (DIR > 0) ww.y = -ww.y;
-          v[i][r] = cmul(v[i][r], ww);
-        };
-        const float2 w1 = __ldg(tw + k * TWS);
-        if constexpr (R == 2) {
-          twiddle(1, w1);
-        } else if constexpr (R == 3 || R == 5) {
-          twiddle(1, w1);
-#pragma unroll
-          for (int r = 2; r < R; r++) twiddle(r, __ldg(tw + r * k * TWS));
-        } else {
-          const float2 w2 = __ldg(tw + 2 * k * TWS);
-          const float2 w3 = (R == 16) ? __ldg(tw + 3 * k * TWS) : cmul(w1, w2);
-          twiddle(1, w1);
-          twiddle(2, w2);
-          twiddle(3, w3);
-#pragma unroll
-          for (int a = 4; a < R; a += 4) {
-            const float2 wa = __ldg(tw + a * k * TWS);
-            twiddle(a, wa);
-            twiddle(a + 1, cmul(R == 16 ? wa : w1, R == 16 ? w1 : wa));
-            twiddle(a + 2, cmul(w2, wa));
-            twiddle(a + 3, cmul(w3, wa));
-          }
-        }
-      }
+      if (NS > 1) apply_twiddles<R, DIR, TWS>(v[i], k, tw);
       dft<R, DIR>(v[i]);
     }
   }
@@ -246,6 +249,43 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
   }
   __syncthreads();
   if constexpr (NS * R < L) fft_pass<L, NB, T, DIR, NS * R>(s, tw);
+}
+
+// block_fft of NB sequences whose elements come from ``load(b, i)`` (element
+// i of sequence b) instead of shared memory: the first pass reads its
+// butterflies straight from the loader, all of a thread's loads before any
+// arithmetic, and writes its outputs to ``s``; the other passes run in shared
+// memory.  Saves one store and one load of every element in shared memory.
+template <int L, int NB, int T, int DIR, typename Load>
+__device__ __forceinline__ void block_fft_from(float2* s, const float2* __restrict__ tw, Load load) {
+  static_assert(L >= 2 && TWN % L == 0, "L must divide the twiddle table length 2^14 * 3 * 5");
+  constexpr int R = fft_radix(L);
+  constexpr int LR = L / R;
+  constexpr int NBF = NB * LR;
+  constexpr int K = (NBF + T - 1) / T;
+  constexpr int LD = ld_of(L);
+  float2 v[K][R];
+#pragma unroll
+  for (int i = 0; i < K; i++) {
+    const int bf = threadIdx.x + i * T;
+    if ((NBF % T) == 0 || bf < NBF) {
+      const int b = bf / LR, j = bf - (bf / LR) * LR;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[i][r] = load(b, j + r * LR);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < K; i++) {
+    const int bf = threadIdx.x + i * T;
+    if ((NBF % T) == 0 || bf < NBF) {
+      const int b = bf / LR, j = bf - (bf / LR) * LR;
+      dft<R, DIR>(v[i]);
+#pragma unroll
+      for (int r = 0; r < R; r++) s[b * LD + pidx(j * R + r)] = v[i][r];
+    }
+  }
+  __syncthreads();
+  if constexpr (R < L) fft_pass<L, NB, T, DIR, R>(s, tw);
 }
 
 // Transform NB sequences of length L in shared memory (natural order in and

@@ -13,27 +13,44 @@
 namespace zr {
 
 constexpr int SS_TX = 64, SS_TY = 16, SS_THR = 256;
+#ifndef ZR_SS_MINB
+#define ZR_SS_MINB 8
+#endif
 
 __device__ __forceinline__ int refl1(int i, int n) { return i < 0 ? -i - 1 : (i >= n ? 2 * n - i - 1 : i); }
 
-__global__ void __launch_bounds__(SS_THR)
+// One raw value of the compile-time type TYPE, as float.
+template <int TYPE>
+__device__ __forceinline__ float raw_at(const void* raw, long long idx) {
+  if constexpr (TYPE == ZR_U8) return (float)__ldg((const uint8_t*)raw + idx);
+  if constexpr (TYPE == ZR_U16) return (float)__ldg((const uint16_t*)raw + idx);
+  if constexpr (TYPE == ZR_F16) return __half2float(__ldg((const __half*)raw + idx));
+  return __ldg((const float*)raw + idx);
+}
+
+// A CTA owns a 64 x 16 output tile and walks the frames in order.  The halo
+// tile of frame n+1 (the corrected values at the rolled, reflected source
+// pixels) is loaded into registers while frame n is filtered; the three
+// running sums live in shared memory, which leaves the registers for the
+// loads in flight at eight resident CTAs per SM.
+template <int TYPE>
+__global__ void __launch_bounds__(SS_THR, ZR_SS_MINB)
     k_shift_sum(FrameSrc f, const zr_shift_t* __restrict__ sh, float* __restrict__ sum,
                 float* __restrict__ even, float* __restrict__ odd, float* __restrict__ aligned) {
   __shared__ float tile[SS_TY + 2][SS_TX + 2];
+  __shared__ float acc[3][SS_TY][SS_TX];  // all frames, even frames, odd frames
   const int x0 = blockIdx.x * SS_TX, y0 = blockIdx.y * SS_TY;
   const int tx = threadIdx.x & (SS_TX - 1), ty = threadIdx.x / SS_TX;  // ty in [0,4)
   constexpr int RPT = SS_TY / (SS_THR / SS_TX);                            // rows per thread (4)
-  float s[RPT], se[RPT], so[RPT];
 #pragma unroll
-  for (int i = 0; i < RPT; i++) s[i] = se[i] = so[i] = 0.0f;
+  for (int i = 0; i < RPT; i++) acc[0][ty * RPT + i][tx] = acc[1][ty * RPT + i][tx] = acc[2][ty * RPT + i][tx] = 0.0f;
   const int H = f.H, W = f.W;
-  // the halo tile of frame n+1 is loaded into registers while frame n is
-  // filtered, so that its loads overlap the arithmetic and the stores
   constexpr int TE = (SS_TY + 2) * (SS_TX + 2);
   constexpr int LPT = (TE + SS_THR - 1) / SS_THR;
   float pre[LPT];
   auto fetch = [&](int n) {
     const zr_shift_t t = sh[n];
+    const long long fo = (long long)n * f.fstride;
 #pragma unroll
     for (int l = 0; l < LPT; l++) {
       const int e = threadIdx.x + l * SS_THR;
@@ -47,7 +64,13 @@ __global__ void __launch_bounds__(SS_THR)
           if (sy < 0) sy += H;
           int sx = X - t.roll_x;
           if (sx < 0) sx += W;
-          pre[l] = load_corrected(f, n, sy, sx);
+          // the corrected value, in the order of load_corrected
+          const long long p = (long long)sy * W + sx;
+          float v = raw_at<TYPE>(f.raw, fo + p);
+          if (f.gain) v = __fmul_rn(__ldg(f.gain + p), v);
+          if (f.gdiv != 0.0f) v = __fdiv_rn(v, f.gdiv);
+          if (f.ha) v = __fmaf_rn(__ldg(f.ha + p), v, __ldg(f.hb + p));
+          pre[l] = v;
         }
       }
     }
@@ -64,6 +87,7 @@ __global__ void __launch_bounds__(SS_THR)
     __syncthreads();
     if (n + 1 < f.N) fetch(n + 1);
     const int x = x0 + tx;
+    float* const half_acc = acc[1 + (n & 1)][0];
 #pragma unroll
     for (int i = 0; i < RPT; i++) {
       const int y = y0 + ty * RPT + i;
@@ -78,8 +102,8 @@ __global__ void __launch_bounds__(SS_THR)
       } else {
         a = tile[ly][lx];
       }
-      s[i] += a;
-      if (n & 1) so[i] += a; else se[i] += a;
+      acc[0][ly - 1][tx] += a;
+      half_acc[(ly - 1) * SS_TX + tx] += a;
       if (aligned && y < H && x < W) aligned[(size_t)n * H * W + (size_t)y * W + x] = a;
     }
   }
@@ -89,9 +113,9 @@ __global__ void __launch_bounds__(SS_THR)
     const int y = y0 + ty * RPT + i;
     if (y < H && x < W) {
       const size_t p = (size_t)y * W + x;
-      sum[p] = s[i];
-      if (even) even[p] = se[i];
-      if (odd) odd[p] = so[i];
+      sum[p] = acc[0][ty * RPT + i][tx];
+      if (even) even[p] = acc[1][ty * RPT + i][tx];
+      if (odd) odd[p] = acc[2][ty * RPT + i][tx];
     }
   }
 }
@@ -106,6 +130,13 @@ extern "C" int zr_shift_sum(const zr_frames_t* frames, const zr_shift_t* shifts,
   FrameSrc f = make_src(frames);
   if (f.N <= 0 || f.H < 2 || f.W < 2) return set_error(ZR_EINVAL, "zr_shift_sum: empty movie");
   dim3 grid((f.W + SS_TX - 1) / SS_TX, (f.H + SS_TY - 1) / SS_TY);
-  k_shift_sum<<<grid, SS_THR, 0, (cudaStream_t)stream>>>(f, shifts, image_sum, even_sum, odd_sum, aligned);
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (f.type) {
+    case ZR_U8: k_shift_sum<ZR_U8><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned); break;
+    case ZR_U16: k_shift_sum<ZR_U16><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned); break;
+    case ZR_F16: k_shift_sum<ZR_F16><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned); break;
+    case ZR_F32: k_shift_sum<ZR_F32><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned); break;
+    default: return set_error(ZR_EINVAL, "zr_shift_sum: raw type %d", f.type);
+  }
   return launched("k_shift_sum");
 }

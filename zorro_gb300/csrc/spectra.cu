@@ -150,20 +150,11 @@ __global__ void __launch_bounds__(fft_threads(P0, NBR), fft_minblocks(P0))
   const int nl = blockIdx.y;
   const float2* R = (blockIdx.z == 0 ? RU : RV) + (size_t)nl * H4 * K4 * NBR;
   float2* out = (blockIdx.z == 0 ? G : S) + (size_t)nl * spec_elems;
-  for (int e = threadIdx.x; e < H4 * NBR * NBR; e += T) {
-    const int gg = e / (NBR * NBR), j = e - gg * (NBR * NBR);
-    const int c = j / NBR, r = j - c * NBR;
-    const int y = gg * NBR + r;
-    float2 v = R[((size_t)gg * K4 + k0) * NBR + j];
-    if (y >= rows) v = make_float2(0.0f, 0.0f);
-    sm[c * LD + pidx(y)] = v;
-  }
-  for (int e = threadIdx.x; e < (P0 - H4 * NBR) * NBR; e += T) {
-    const int c = e / (P0 - H4 * NBR), y = H4 * NBR + e - c * (P0 - H4 * NBR);
-    sm[c * LD + pidx(y)] = make_float2(0.0f, 0.0f);
-  }
-  __syncthreads();
-  block_fft<P0, NBR, T, -1>(sm, tw);
+  // element y of column k0 + c: row y of the row-pass output, zero past the
+  // frame (the zero padding to P0)
+  block_fft_from<P0, NBR, T, -1>(sm, tw, [&](int c, int y) {
+    return y < rows ? __ldg(R + ((size_t)(y >> 2) * K4 + k0 + c) * NBR + (y & 3)) : make_float2(0.0f, 0.0f);
+  });
   const int hc = C0 / 2;
   const int RP = C0 + 4;
   for (int e = threadIdx.x; e < (C0 + 1) * NBR; e += T) {

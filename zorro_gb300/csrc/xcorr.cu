@@ -27,14 +27,19 @@
 
 namespace zr {
 
+// Column pass: columns per CTA (fewer for the long 3072 and 4096 columns)
+// and threads (ZR_XC_EPT elements per thread and pass).
+#ifndef ZR_XC_NBC
+#define ZR_XC_NBC 4
+#endif
 #ifndef ZR_XC_EPT
 #define ZR_XC_EPT 32
 #endif
-constexpr int XC_NBC = 4;  // columns per CTA in the column pass
-// elements per thread of the column-pass transforms (two radix-16 butterflies
-// per thread and pass): 256 threads of <= 128 registers for a 2048-point
-// crop, two CTAs per SM; measured faster than one butterfly per thread
-constexpr int XC_EPT = ZR_XC_EPT;
+#ifndef ZR_XC_MINB
+#define ZR_XC_MINB 2
+#endif
+__host__ __device__ constexpr int xc_nbc(int C0) { return C0 >= 3072 ? 1 : ZR_XC_NBC; }
+__host__ __device__ constexpr int xc_threads(int C0) { return fft_threads(C0, xc_nbc(C0), ZR_XC_EPT); }
 constexpr int XC_NBR = 2;  // packed row pairs per CTA in the row pass
 
 struct XcJobs {
@@ -79,88 +84,111 @@ __device__ __forceinline__ void job_operands(const XcJobs& J, int job, const E*&
   unscale = J.sc ? 1.0f / (J.sc[ia] * J.sc[ib]) : 1.0f;
 }
 
-// Two consecutive complex values of a spectrum column, and one value.
-__device__ __forceinline__ float4 load_pair(const float2* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
-__device__ __forceinline__ float4 load_pair(const __half2* p) {
-  const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
-  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
-  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
-  return make_float4(a.x, a.y, b.x, b.y);
-}
-__device__ __forceinline__ float2 load_one(const float2* p) { return *p; }
-__device__ __forceinline__ float2 load_one(const __half2* p) { return __half22float2(*p); }
+// One complex value of a spectrum.
+__device__ __forceinline__ float2 load_one(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 load_one(const __half2* p) { return __half22float2(__ldg(p)); }
+__device__ __forceinline__ float2 to_f2(float2 a) { return a; }
+__device__ __forceinline__ float2 to_f2(__half2 a) { return __half22float2(a); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
+// Value of the cropped product A conj(B) at row ``row`` of column k, as the
+// full C0 x C1 product contributes to real(IFFT): regular columns as they
+// are, except that row C0/2 averages the -C0/2 and +C0/2 products (the
+// latter stored at index C0 of the column); the Nyquist column C1/2 holds
+// conj(A) B of the mirrored row; columns past it are zero.
 template <int C0, typename E>
-__global__ void __launch_bounds__(fft_threads(C0, XC_NBC, XC_EPT), fft_minblocks(C0))
+__device__ __forceinline__ float2 xc_product(const E* a, const E* b, int row, int k, int half, float us) {
+  constexpr int hc = C0 / 2;
+  float2 h = make_float2(0.0f, 0.0f);
+  if (k < half) {
+    h = cmulc(load_one(a + row), load_one(b + row));
+    if (k > 0 && row == hc) {
+      const float2 h2 = cmulc(load_one(a + C0), load_one(b + C0));
+      h = make_float2(0.5f * (h.x + h2.x), 0.5f * (h.y + h2.y));
+    }
+  } else if (k == half) {
+    const int m = row == 0 ? 0 : (row == hc ? C0 : C0 - row);
+    h = cmulc(load_one(b + m), load_one(a + m));
+  }
+  if (sizeof(E) != sizeof(float2)) h = cscale(h, us);  // undo the power-of-two scales (exact)
+  return h;
+}
+
+// Column pass: CTA (job, column group) transforms xc_nbc(C0) columns of the
+// job's product.  Jobs vary fastest across the grid, so the CTAs resident at
+// one time read the same columns of every spectrum and share them through L2.
+// The first radix-16 pass forms the products while it loads its butterflies
+// from the (column-major) spectra, so no product buffer passes through shared
+// memory; the other passes run in shared memory, and the window rows
+// [-maxShift, ...) of the result are kept.
+template <int C0, typename E>
+__global__ void __launch_bounds__(xc_threads(C0), ZR_XC_MINB)
     k_xc_cols(XcJobs J, int C1, int K4, int mS, float2* __restrict__ Tw, const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(C0, XC_NBC, XC_EPT);
+  constexpr int NBC = xc_nbc(C0);
+  constexpr int T = xc_threads(C0);
   constexpr int LD = ld_of(C0);
+  constexpr int RP = C0 + 4;  // column pitch of the spectra
+  constexpr int R = fft_radix(C0);
+  constexpr int LR = C0 / R;
+  constexpr int NBF = NBC * LR;
+  constexpr int K = (NBF + T - 1) / T;
+  static_assert(R < C0, "at least two passes");
   extern __shared__ float2 sm[];
-  // jobs vary fastest across the grid so that the CTAs resident at one time
-  // share the same column tile of every spectrum through L2
-  const int k0 = blockIdx.y * XC_NBC;
+  const int k0 = blockIdx.y * NBC;
   const int jl = blockIdx.x;
   const E *A, *B;
   float us;
   job_operands(J, J.job0 + jl, A, B, us);
-  const int half = C1 / 2, hc = C0 / 2;
-  const int RP = C0 + 4;  // column pitch of the spectra
-  // two rows per element: 16-byte loads along each (contiguous) column.  The
-  // regular columns (0 <= k < C1/2) load XC_UNR element pairs before using any,
-  // so that several loads per thread are in flight.
-  constexpr int NE = (C0 / 2) * XC_NBC;  // element pairs per CTA
-  constexpr int XC_UNR = 4;
-  for (int e0 = threadIdx.x; e0 < NE; e0 += T * XC_UNR) {
-    float4 av[XC_UNR], bv[XC_UNR];
+  const int half = C1 / 2;
+  float2 v[K][R];
 #pragma unroll
-    for (int u = 0; u < XC_UNR; u++) {
-      const int e = e0 + u * T;
-      av[u] = bv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (e < NE) {
-        const int c = e / (C0 / 2), r = 2 * (e - c * (C0 / 2));
-        const int k = k0 + c;
-        if (k < half) {
-          av[u] = load_pair(A + (size_t)k * RP + r);
-          bv[u] = load_pair(B + (size_t)k * RP + r);
-        }
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < XC_UNR; u++) {
-      const int e = e0 + u * T;
-      if (e >= NE) continue;
-      const int c = e / (C0 / 2), r = 2 * (e - c * (C0 / 2));
-      const int k = k0 + c;
-      float2 h0 = make_float2(0.0f, 0.0f), h1 = h0;
+  for (int i = 0; i < K; i++) {
+    const int bf = threadIdx.x + i * T;
+    if ((NBF % T) == 0 || bf < NBF) {
+      const int b = bf / LR, j = bf - b * LR;
+      const int k = k0 + b;
+      const E* a = A + (size_t)k * RP;
+      const E* bb = B + (size_t)k * RP;
       if (k < half) {
-        h0 = cmulc(make_float2(av[u].x, av[u].y), make_float2(bv[u].x, bv[u].y));
-        h1 = cmulc(make_float2(av[u].z, av[u].w), make_float2(bv[u].z, bv[u].w));
-        if (k > 0 && r == hc) {
-          const float2 h2 = cmulc(load_one(A + (size_t)k * RP + C0), load_one(B + (size_t)k * RP + C0));
-          h0 = make_float2(0.5f * (h0.x + h2.x), 0.5f * (h0.y + h2.y));
+        // every load of the butterfly first (all in bounds), then the products
+        E av[R], bv[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          av[r] = __ldg(a + j + r * LR);
+          bv[r] = __ldg(bb + j + r * LR);
         }
-      } else if (k == half) {
-        const E* Ak = A + (size_t)k * RP;
-        const E* Bk = B + (size_t)k * RP;
-        const int m0 = (r == 0) ? 0 : (r == hc ? C0 : C0 - r), m1 = C0 - r - 1;
-        h0 = cmulc(load_one(Bk + m0), load_one(Ak + m0));  // conj(A) * B at the mirrored row
-        h1 = cmulc(load_one(Bk + m1), load_one(Ak + m1));
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          float2 h = cmulc(to_f2(av[r]), to_f2(bv[r]));
+          if (k > 0 && j + r * LR == C0 / 2) {  // row -C0/2: average with the +C0/2 product
+            const float2 h2 = cmulc(load_one(a + C0), load_one(bb + C0));
+            h = make_float2(0.5f * (h.x + h2.x), 0.5f * (h.y + h2.y));
+          }
+          if (sizeof(E) != sizeof(float2)) h = cscale(h, us);  // undo the power-of-two scales (exact)
+          v[i][r] = h;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) v[i][r] = xc_product<C0>(a, bb, j + r * LR, k, half, us);
       }
-      if (sizeof(E) != sizeof(float2)) {  // undo the power-of-two scales (exact)
-        h0 = cscale(h0, us);
-        h1 = cscale(h1, us);
-      }
-      sm[c * LD + pidx(r)] = h0;
-      sm[c * LD + pidx(r + 1)] = h1;
+      dft<R, 1>(v[i]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < K; i++) {
+    const int bf = threadIdx.x + i * T;
+    if ((NBF % T) == 0 || bf < NBF) {
+      const int b = bf / LR, j = bf - b * LR;
+#pragma unroll
+      for (int r = 0; r < R; r++) sm[b * LD + pidx(j * R + r)] = v[i][r];
     }
   }
   __syncthreads();
-  block_fft<C0, XC_NBC, T, 1>(sm, tw);
   const int rows = J.rows;
   float2* out = Tw + (size_t)jl * rows * K4;
-  for (int e = threadIdx.x; e < rows * XC_NBC; e += T) {
-    const int a = e / XC_NBC, c = e - a * XC_NBC;
+  fft_pass<C0, NBC, T, 1, R>(sm, tw);
+  for (int e = threadIdx.x; e < rows * NBC; e += T) {
+    const int a = e / NBC, c = e - a * NBC;
     const int y = a < mS ? a - mS + C0 : a - mS;
     out[(size_t)a * K4 + k0 + c] = sm[c * LD + pidx(y)];
   }
@@ -234,11 +262,12 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
 template <int C0, typename E>
 static int launch_xc_cols_t(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
                             cudaStream_t st) {
-  constexpr int T = fft_threads(C0, XC_NBC, XC_EPT);
-  const size_t smem = (size_t)XC_NBC * ld_of(C0) * sizeof(float2);
+  constexpr int T = xc_threads(C0);
+  constexpr int NBC = xc_nbc(C0);
+  const size_t smem = (size_t)NBC * ld_of(C0) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_xc_cols attr"));
-  k_xc_cols<C0, E><<<dim3(nj, K4 / XC_NBC), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
+  k_xc_cols<C0, E><<<dim3(nj, K4 / NBC), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
   return launched("k_xc_cols");
 }
 
