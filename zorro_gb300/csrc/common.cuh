@@ -160,4 +160,19 @@ __device__ __forceinline__ float4 finish4(const FrameSrc& f, const Px4& q) {
 
 __device__ __forceinline__ int ilog2c(int v) { return 31 - __clz(v); }
 
+// Element i of the length-L complex sequence whose inverse FFT holds two real
+// rows (row a in the real part, row b in the imaginary part), from the rows'
+// half-plane spectra ``ra``/``rb`` (elements 0..L/2; null: a zero row):
+// ga + i gb up to L/2, the Hermitian mirror conj(ga) + i conj(gb) above.
+template <int L>
+__device__ __forceinline__ float2 packed_rows(const float2* __restrict__ ra, const float2* __restrict__ rb, int i) {
+  constexpr int half = L / 2;
+  const int k = i <= half ? i : L - i;
+  const float2 ga = ra ? __ldg(ra + k) : make_float2(0.0f, 0.0f);
+  const float2 gb = rb ? __ldg(rb + k) : make_float2(0.0f, 0.0f);
+  if (i == 0 || i == half) return make_float2(ga.x, gb.x);
+  if (i < half) return make_float2(ga.x - gb.y, ga.y + gb.x);
+  return make_float2(ga.x + gb.y, -ga.y + gb.x);
+}
+
 }  // namespace zr

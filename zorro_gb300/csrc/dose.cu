@@ -127,15 +127,9 @@ __global__ void __launch_bounds__(DS_CT, 2)
   }
   const float LOG2E = 1.4426950408889634f;
   for (int nl = 0; nl < nfr; nl++) {
-    const float4* col = reinterpret_cast<const float4*>(RW + ((size_t)nl * K4 + kx) * P0);
-    __syncthreads();
-    for (int e = threadIdx.x; e < P0 / 2; e += DS_CT) {
-      const float4 v = col[e];
-      sm[pidx(2 * e)] = make_float2(v.x, v.y);
-      sm[pidx(2 * e + 1)] = make_float2(v.z, v.w);
-    }
-    __syncthreads();
-    block_fft<P0, 1, DS_CT, -1>(sm, tw);
+    const float2* col = RW + ((size_t)nl * K4 + kx) * P0;
+    __syncthreads();  // the previous frame's spectrum has been read
+    block_fft_from<P0, 1, DS_CT, -1>(sm, tw, [&](int, int y) { return __ldg(col + y); });
     if (!live) continue;
     // filt = exp(-0.5 D / crit), thres = exp(-(q / thresQ)^order)
     const float cd = (-0.5f * dose_end[f0 + nl]) * LOG2E;
@@ -168,17 +162,14 @@ __global__ void __launch_bounds__(fft_threads(P0, DS_NBR), fft_minblocks(P0))
   constexpr int LD = ld_of(P0);
   extern __shared__ float2 sm[];
   const int k0 = blockIdx.x * DS_NBR;
-  for (int e = threadIdx.x; e < DS_NBR * P0; e += T) {
-    const int c = e / P0, y = e - c * P0;
-    float2 v = ACC[(size_t)(k0 + c) * P0 + y];
+  block_fft_from<P0, DS_NBR, T, 1>(sm, tw, [&](int c, int y) {
+    float2 v = __ldg(ACC + (size_t)(k0 + c) * P0 + y);
     if (normalize) {
-      const float s = 1.0f / (FM[(size_t)(k0 + c) * P0 + y] + 1.0f);
+      const float s = 1.0f / (__ldg(FM + (size_t)(k0 + c) * P0 + y) + 1.0f);
       v = make_float2(v.x * s, v.y * s);
     }
-    sm[c * LD + pidx(y)] = v;
-  }
-  __syncthreads();
-  block_fft<P0, DS_NBR, T, 1>(sm, tw);
+    return v;
+  });
   for (int e = threadIdx.x; e < H * DS_NBR; e += T) {
     const int y = e / DS_NBR, c = e - y * DS_NBR;
     T2[(size_t)y * K4 + k0 + c] = sm[c * LD + pidx(y)];
@@ -192,24 +183,12 @@ __global__ void __launch_bounds__(fft_threads(P1, 2), fft_minblocks(P1))
                  const float2* __restrict__ tw) {
   constexpr int T = fft_threads(P1, 2);
   constexpr int LD = ld_of(P1);
-  constexpr int half = P1 / 2;
   extern __shared__ float2 sm[];
   const int y0 = blockIdx.x * 4;
-  for (int e = threadIdx.x; e < 2 * (half + 1); e += T) {
-    const int p = e / (half + 1), k = e - p * (half + 1);
+  block_fft_from<P1, 2, T, 1>(sm, tw, [&](int p, int i) {
     const int a0 = y0 + 2 * p, a1 = a0 + 1;
-    const float2 ga = a0 < H ? T2[(size_t)a0 * K4 + k] : make_float2(0.0f, 0.0f);
-    const float2 gb = a1 < H ? T2[(size_t)a1 * K4 + k] : make_float2(0.0f, 0.0f);
-    float2* s = sm + p * LD;
-    if (k == 0 || k == half) {
-      s[pidx(k)] = make_float2(ga.x, gb.x);
-    } else {
-      s[pidx(k)] = make_float2(ga.x - gb.y, ga.y + gb.x);
-      s[pidx(P1 - k)] = make_float2(ga.x + gb.y, -ga.y + gb.x);
-    }
-  }
-  __syncthreads();
-  block_fft<P1, 2, T, 1>(sm, tw);
+    return packed_rows<P1>(a0 < H ? T2 + (size_t)a0 * K4 : nullptr, a1 < H ? T2 + (size_t)a1 * K4 : nullptr, i);
+  });
   for (int e = threadIdx.x; e < 4 * W; e += T) {
     const int q = e / W, x = e - q * W;
     const int y = y0 + q;

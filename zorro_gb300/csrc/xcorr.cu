@@ -200,7 +200,6 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
               const float* __restrict__ terms, float* __restrict__ out, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(C1, XC_NBR);
   constexpr int LD = ld_of(C1);
-  constexpr int half = C1 / 2;
   extern __shared__ float2 sm[];
   const int w = 2 * mS;
   const int rows = J.rows;  // w + 1 for the frame terms (rows and columns -mS..mS)
@@ -208,21 +207,10 @@ __global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
   const int job = J.job0 + jl;
   const int arow0 = blockIdx.x * (2 * XC_NBR);
   const float2* src = Tw + (size_t)jl * rows * K4;
-  for (int e = threadIdx.x; e < XC_NBR * (half + 1); e += T) {
-    const int p = e / (half + 1), k = e - p * (half + 1);
+  block_fft_from<C1, XC_NBR, T, 1>(sm, tw, [&](int p, int i) {
     const int a0 = arow0 + 2 * p, a1 = a0 + 1;
-    const float2 ga = a0 < rows ? src[(size_t)a0 * K4 + k] : make_float2(0.0f, 0.0f);
-    const float2 gb = a1 < rows ? src[(size_t)a1 * K4 + k] : make_float2(0.0f, 0.0f);
-    float2* s = sm + p * LD;
-    if (k == 0 || k == half) {
-      s[pidx(k)] = make_float2(ga.x, gb.x);
-    } else {
-      s[pidx(k)] = make_float2(ga.x - gb.y, ga.y + gb.x);           // ga + i gb
-      s[pidx(C1 - k)] = make_float2(ga.x + gb.y, -ga.y + gb.x);     // conj(ga) + i conj(gb)
-    }
-  }
-  __syncthreads();
-  block_fft<C1, XC_NBR, T, 1>(sm, tw);
+    return packed_rows<C1>(a0 < rows ? src + (size_t)a0 * K4 : nullptr, a1 < rows ? src + (size_t)a1 * K4 : nullptr, i);
+  });
   const size_t w2 = (size_t)w * w;
   const int cols = rows;  // the terms window is square, w + 1 wide
   for (int e = threadIdx.x; e < XC_NBR * 2 * cols; e += T) {

@@ -9,6 +9,8 @@ follows.  The GPU does every pass over pixels.
 """
 from __future__ import annotations
 
+import concurrent.futures
+
 import numpy as np
 import scipy.optimize
 import scipy.special
@@ -166,8 +168,12 @@ def solve_shifts(shiftsTriMat_in, corrTriMat_in, peaksigTriMat_in, *, shapeImage
     lim = np.min([shapeImage[0] / 2.0, shapeImage[1] / 2.0] + ([] if maxShift is None else [N * maxShift]))
     rel = np.zeros([N, 2])
     weff = weights * accepted
-    rel[:, 1] = l1_solve(A, b_x, weff, -lim, lim)
-    rel[:, 0] = l1_solve(A, b_y, weff, -lim, lim)
+    # the x and y solves are independent: y on a helper thread (the native
+    # solver releases the GIL) while x runs here
+    with concurrent.futures.ThreadPoolExecutor(1) as ex:
+        fy = ex.submit(l1_solve, A, b_y, weff, -lim, lim)
+        rel[:, 1] = l1_solve(A, b_x, weff, -lim, lim)
+        rel[:, 0] = fy.result()
     # weighted error analysis, zorro.py:1484-1547
     weights = np.clip(weights, 1e-6, np.inf)
     errorXY = np.stack([A @ rel[:, 0] - b_y, A @ rel[:, 1] - b_x], axis=1)
@@ -282,36 +288,48 @@ def hotpix_bins(sumMean, maxSigma):
     return sumMean, poissonStd, edges
 
 
+def _memo_last(f):
+    """f remembering its value at the last point it was called with:
+    L-BFGS-B asks for f and then for the gradient at the same point."""
+    last = [None, None]
+
+    def fm(x):
+        key = tuple(float(v) for v in np.asarray(x).ravel())
+        if last[0] != key:
+            last[0], last[1] = key, f(np.array(key))
+        return last[1]
+    return fm
+
+
 def _forward_difference(f, bounds, step=1e-8):
     """The gradient L-BFGS-B estimates when no jac is given (scipy's 2-point
     approx_derivative with absolute step ``step``, the steps turned around or
     shortened to stay inside ``bounds``), as a jac callable: the same
-    numbers without the general machinery's per-call overhead."""
-    lb = np.array([b[0] for b in bounds], dtype=np.float64)
-    ub = np.array([b[1] for b in bounds], dtype=np.float64)
-    eps2 = np.finfo(np.float64).eps ** 0.5
+    numbers (the same float64 operations on Python floats) without the
+    general machinery's per-call overhead."""
+    lb = [float(b[0]) for b in bounds]
+    ub = [float(b[1]) for b in bounds]
+    eps2 = float(np.finfo(np.float64).eps ** 0.5)
 
     def grad(x):
-        x0 = np.asarray(x, dtype=np.float64)
-        f0 = f(x0)
-        sign_x0 = (x0 >= 0).astype(np.float64) * 2 - 1
-        h = np.full(x0.shape, step)
-        dx = (x0 + h) - x0
-        h = np.where(dx == 0, eps2 * sign_x0 * np.maximum(1.0, np.abs(x0)), h)
-        lower_dist, upper_dist = x0 - lb, ub - x0
-        xs = x0 + h
-        violated = (xs < lb) | (xs > ub)
-        fitting = np.abs(h) <= np.maximum(lower_dist, upper_dist)
-        h[violated & fitting] *= -1
-        forward = (upper_dist >= lower_dist) & ~fitting
-        h[forward] = upper_dist[forward]
-        backward = (upper_dist < lower_dist) & ~fitting
-        h[backward] = -lower_dist[backward]
-        g = np.empty_like(x0)
-        for i in range(x0.size):
-            x1 = x0.copy()
-            x1[i] = x0[i] + h[i]
-            g[i] = (f(x1) - f0) / ((x0[i] + h[i]) - x0[i])
+        x0 = [float(v) for v in np.asarray(x).ravel()]
+        f0 = f(np.array(x0))
+        g = np.empty(len(x0))
+        for i, xi in enumerate(x0):
+            h = step
+            if (xi + h) - xi == 0.0:
+                h = eps2 * (1.0 if xi >= 0 else -1.0) * max(1.0, abs(xi))
+            lower_dist, upper_dist = xi - lb[i], ub[i] - xi
+            xs = xi + h
+            violated = xs < lb[i] or xs > ub[i]
+            fitting = abs(h) <= max(lower_dist, upper_dist)
+            if violated and fitting:
+                h = -h
+            elif not fitting:
+                h = upper_dist if upper_dist >= lower_dist else -lower_dist
+            x1 = list(x0)
+            x1[i] = xi + h
+            g[i] = (f(np.array(x1)) - f0) / ((xi + h) - xi)
         return g
     return grad
 
@@ -333,8 +351,9 @@ def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
         return np.sum(np.abs(cdf - scipy.special.ndtr((counts - params[0]) / params[1])))
 
     bounds = ((sumMean - 0.5 * poissonStd, sumMean + 0.5 * poissonStd), (0.7 * poissonStd, 1.3 * poissonStd))
-    best = scipy.optimize.minimize(err, (sumMean, poissonStd), method="L-BFGS-B", bounds=bounds,
-                                   jac=_forward_difference(err, bounds))
+    errm = _memo_last(err)
+    best = scipy.optimize.minimize(errm, (sumMean, poissonStd), method="L-BFGS-B", bounds=bounds,
+                                   jac=_forward_difference(errm, bounds))
     with np.errstate(all="ignore"):
         sig_cdf = np.sqrt(2) * scipy.special.erfinv(2.0 * cdf - 1)
     normal = (counts - best.x[0]) / best.x[1]
