@@ -18,7 +18,14 @@
 
 namespace zr {
 
-constexpr int DS_NBR = 4;  // rows per CTA (forward row pass)
+// rows per CTA of the forward row pass and columns per CTA of the inverse
+// column pass
+#ifndef ZR_DS_NBR
+#define ZR_DS_NBR 4
+#endif
+constexpr int DS_NBR = ZR_DS_NBR;
+// CTAs per SM to ask the register allocator for: 128 registers a thread
+constexpr int ds_minb(int T) { return T >= 512 ? 1 : 512 / T; }
 
 
 __device__ __forceinline__ int sym_idx(int i, int n) {
@@ -27,7 +34,7 @@ __device__ __forceinline__ int sym_idx(int i, int n) {
 }
 
 template <int P1>
-__global__ void __launch_bounds__(fft_threads(P1, DS_NBR), fft_minblocks(P1))
+__global__ void __launch_bounds__(fft_threads(P1, DS_NBR), ds_minb(fft_threads(P1, DS_NBR)))
     k_dose_rows(const float* __restrict__ img, int N, int H, int W, int f0, int K4, int P0,
                 float2* __restrict__ RW, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(P1, DS_NBR);
@@ -155,7 +162,7 @@ __global__ void __launch_bounds__(DS_CT, 2)
 
 // Inverse column pass, keeping rows [0, H).
 template <int P0>
-__global__ void __launch_bounds__(fft_threads(P0, DS_NBR), fft_minblocks(P0))
+__global__ void __launch_bounds__(fft_threads(P0, DS_NBR), ds_minb(fft_threads(P0, DS_NBR)))
     k_dose_icols(const float2* __restrict__ ACC, const float* __restrict__ FM, int normalize, int K4, int H,
                  float2* __restrict__ T2, const float2* __restrict__ tw) {
   constexpr int T = fft_threads(P0, DS_NBR);

@@ -16,14 +16,24 @@
 
 namespace zr {
 
-constexpr int NBR = 4;  // rows / columns per CTA
+constexpr int NBR = 4;  // rows per group of the row-pass output layout
+// rows per CTA of the row pass and columns per CTA of the column pass
+#ifndef ZR_FR_ROWS
+#define ZR_FR_ROWS 2
+#endif
+#ifndef ZR_FC_COLS
+#define ZR_FC_COLS 2
+#endif
+constexpr int FR = ZR_FR_ROWS, FC = ZR_FC_COLS;
+// CTAs per SM to ask the register allocator for: 128 registers a thread
+constexpr int minb_of(int T) { return T >= 512 ? 1 : 512 / T; }
 
 template <int P1>
-__global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
+__global__ void __launch_bounds__(fft_threads(P1, FR), minb_of(fft_threads(P1, FR)))
     k_fwd_rows(FrameSrc f, const float* __restrict__ mask, const double* __restrict__ mean_sub,
                double inv_area, int frame0, int mode, int rows, int cols, int C1, int K4, int H4,
                float2* __restrict__ RU, float2* __restrict__ RV, const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(P1, NBR);
+  constexpr int T = fft_threads(P1, FR);
   constexpr int LD = ld_of(P1);
   extern __shared__ float2 sm[];
   // frames vary fastest so that concurrent CTAs read the same rows of the
@@ -38,7 +48,7 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
     // every map; the unaligned head (< 4 pixels) and tail go pixel by pixel
     // FR_UNR quads per thread are fetched before any is used, so that several
     // loads per thread are in flight
-    constexpr int NQ = NBR * (P1 / 4);
+    constexpr int NQ = FR * (P1 / 4);
     constexpr int FR_UNR = 4;
     for (int e0 = threadIdx.x; e0 < NQ; e0 += T * FR_UNR) {
       Px4 px[FR_UNR];
@@ -47,7 +57,7 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
         const int e = e0 + u * T;
         if (e < NQ) {
           const int r = e / (P1 / 4), q = e - r * (P1 / 4);
-          const int y = g * NBR + r;
+          const int y = g * FR + r;
           if (y < rows) {
             const long long p0 = (long long)y * f.W;
             const int x = (int)((4 - (p0 & 3)) & 3) + 4 * q;
@@ -60,7 +70,7 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
         const int e = e0 + u * T;
         if (e >= NQ) continue;
         const int r = e / (P1 / 4), q = e - r * (P1 / 4);
-        const int y = g * NBR + r;
+        const int y = g * FR + r;
         float2* srow = sm + r * LD;
         if (y >= rows) {
 #pragma unroll
@@ -104,9 +114,9 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
       }
     }
   } else {
-    for (int e = threadIdx.x; e < NBR * P1; e += T) {
+    for (int e = threadIdx.x; e < FR * P1; e += T) {
       const int r = e / P1, x = e - (e / P1) * P1;
-      const int y = g * NBR + r;
+      const int y = g * FR + r;
       float2 z = make_float2(0.0f, 0.0f);
       if (y < rows && x < cols) {
         const float m = mask ? __ldg(mask + (size_t)y * P1 + x) : 1.0f;
@@ -121,11 +131,12 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
     }
   }
   __syncthreads();
-  block_fft<P1, NBR, T, -1>(sm, tw);
-  const size_t base = ((size_t)nl * H4 + g) * K4 * NBR;
+  block_fft<P1, FR, T, -1>(sm, tw);
   const int half = C1 / 2;
-  for (int e = threadIdx.x; e < K4 * NBR; e += T) {
-    const int k = e / NBR, r = e - (e / NBR) * NBR;
+  for (int e = threadIdx.x; e < K4 * FR; e += T) {
+    const int k = e / FR, r = e - (e / FR) * FR;
+    const int y = g * FR + r;
+    const size_t o = (((size_t)nl * H4 + (y >> 2)) * K4 + k) * NBR + (y & 3);
     float2 U = make_float2(0.0f, 0.0f), V = U;
     if (k <= half) {
       const float2 zk = sm[r * LD + pidx(k)];
@@ -133,31 +144,31 @@ __global__ void __launch_bounds__(fft_threads(P1, NBR), fft_minblocks(P1))
       U = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
       V = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
     }
-    RU[base + e] = U;
-    if (mode == 0) RV[base + e] = V;
+    RU[o] = U;
+    if (mode == 0) RV[o] = V;
   }
 }
 
 template <int P0>
-__global__ void __launch_bounds__(fft_threads(P0, NBR), fft_minblocks(P0))
+__global__ void __launch_bounds__(fft_threads(P0, FC), minb_of(fft_threads(P0, FC)))
     k_fwd_cols(const float2* __restrict__ RU, const float2* __restrict__ RV, int rows, int C0, int K4, int H4,
                long long spec_elems, float2* __restrict__ G, float2* __restrict__ S,
                const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(P0, NBR);
+  constexpr int T = fft_threads(P0, FC);
   constexpr int LD = ld_of(P0);
   extern __shared__ float2 sm[];
-  const int k0 = blockIdx.x * NBR;
+  const int k0 = blockIdx.x * FC;
   const int nl = blockIdx.y;
   const float2* R = (blockIdx.z == 0 ? RU : RV) + (size_t)nl * H4 * K4 * NBR;
   float2* out = (blockIdx.z == 0 ? G : S) + (size_t)nl * spec_elems;
   // element y of column k0 + c: row y of the row-pass output, zero past the
   // frame (the zero padding to P0)
-  block_fft_from<P0, NBR, T, -1>(sm, tw, [&](int c, int y) {
+  block_fft_from<P0, FC, T, -1>(sm, tw, [&](int c, int y) {
     return y < rows ? __ldg(R + ((size_t)(y >> 2) * K4 + k0 + c) * NBR + (y & 3)) : make_float2(0.0f, 0.0f);
   });
   const int hc = C0 / 2;
   const int RP = C0 + 4;
-  for (int e = threadIdx.x; e < (C0 + 1) * NBR; e += T) {
+  for (int e = threadIdx.x; e < (C0 + 1) * FC; e += T) {
     const int c = e / (C0 + 1), r = e - c * (C0 + 1);
     const int ky = r < hc ? r : (r < C0 ? P0 - C0 + r : hc);
     out[(size_t)(k0 + c) * RP + r] = sm[c * LD + pidx(ky)];
@@ -192,11 +203,11 @@ template <int P>
 static int launch_rows(const FrameSrc& f, const float* mask, const double* mean_sub, double inv_area,
                        int frame0, int nfr, int mode, int rows, int cols, int C1, int K4, int H4,
                        float2* RU, float2* RV, const float2* tw, cudaStream_t st) {
-  constexpr int T = fft_threads(P, NBR);
-  const size_t smem = (size_t)NBR * ld_of(P) * sizeof(float2);
+  constexpr int T = fft_threads(P, FR);
+  const size_t smem = (size_t)FR * ld_of(P) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_rows<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_fwd_rows attr"));
-  k_fwd_rows<P><<<dim3(nfr, H4), T, smem, st>>>(f, mask, mean_sub, inv_area, frame0, mode, rows, cols, C1, K4,
+  k_fwd_rows<P><<<dim3(nfr, (rows + FR - 1) / FR), T, smem, st>>>(f, mask, mean_sub, inv_area, frame0, mode, rows, cols, C1, K4,
                                                  H4, RU, RV, tw);
   return launched("k_fwd_rows");
 }
@@ -204,11 +215,11 @@ static int launch_rows(const FrameSrc& f, const float* mask, const double* mean_
 template <int P>
 static int launch_cols(const float2* RU, const float2* RV, int rows, int C0, int K4, int H4, long long se,
                        int nfr, int nz, float2* G, float2* S, const float2* tw, cudaStream_t st) {
-  constexpr int T = fft_threads(P, NBR);
-  const size_t smem = (size_t)NBR * ld_of(P) * sizeof(float2);
+  constexpr int T = fft_threads(P, FC);
+  const size_t smem = (size_t)FC * ld_of(P) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_cols<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_fwd_cols attr"));
-  k_fwd_cols<P><<<dim3(K4 / NBR, nfr, nz), T, smem, st>>>(RU, RV, rows, C0, K4, H4, se, G, S, tw);
+  k_fwd_cols<P><<<dim3(K4 / FC, nfr, nz), T, smem, st>>>(RU, RV, rows, C0, K4, H4, se, G, S, tw);
   return launched("k_fwd_cols");
 }
 

@@ -40,7 +40,16 @@ namespace zr {
 #endif
 __host__ __device__ constexpr int xc_nbc(int C0) { return C0 >= 3072 ? 1 : ZR_XC_NBC; }
 __host__ __device__ constexpr int xc_threads(int C0) { return fft_threads(C0, xc_nbc(C0), ZR_XC_EPT); }
-constexpr int XC_NBR = 2;  // packed row pairs per CTA in the row pass
+// Row pass: packed row pairs per CTA, elements per thread and pass
+#ifndef ZR_XR_NBR
+#define ZR_XR_NBR 2
+#endif
+#ifndef ZR_XR_EPT
+#define ZR_XR_EPT 32
+#endif
+constexpr int XC_NBR = ZR_XR_NBR;
+__host__ __device__ constexpr int xr_threads(int C1) { return fft_threads(C1, XC_NBR, ZR_XR_EPT); }
+__host__ __device__ constexpr int xr_minb(int T) { return T >= 512 ? 1 : 512 / T; }
 
 struct XcJobs {
   const void* G;     // spectra: float2, or __half2 when ``sc`` is set
@@ -195,10 +204,10 @@ __global__ void __launch_bounds__(xc_threads(C0), ZR_XC_MINB)
 }
 
 template <int C1>
-__global__ void __launch_bounds__(fft_threads(C1, XC_NBR), fft_minblocks(C1))
+__global__ void __launch_bounds__(xr_threads(C1), xr_minb(xr_threads(C1)))
     k_xc_rows(XcJobs J, int C0, int K4, int mS, float scale, const float2* __restrict__ Tw,
               const float* __restrict__ terms, float* __restrict__ out, const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(C1, XC_NBR);
+  constexpr int T = xr_threads(C1);
   constexpr int LD = ld_of(C1);
   extern __shared__ float2 sm[];
   const int w = 2 * mS;
@@ -269,7 +278,7 @@ static int launch_xc_cols(const XcJobs& J, int nj, int C1, int K4, int mS, float
 template <int C1>
 static int launch_xc_rows(const XcJobs& J, int nj, int C0, int K4, int mS, float scale, const float2* Tw,
                           const float* terms, float* out, const float2* tw, cudaStream_t st) {
-  constexpr int T = fft_threads(C1, XC_NBR);
+  constexpr int T = xr_threads(C1);
   const size_t smem = (size_t)XC_NBR * ld_of(C1) * sizeof(float2);
   ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_rows<C1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "k_xc_rows attr"));
