@@ -192,13 +192,19 @@ def solve_shifts(shiftsTriMat_in, corrTriMat_in, peaksigTriMat_in, *, shapeImage
     ex = np.pad(unravel(np.abs(errorXY[:, 1])), ((0, 1), (1, 0))) * acc
     ey = np.pad(unravel(np.abs(errorXY[:, 0])), ((0, 1), (1, 0))) * acc
     wu = np.pad(unravel(weights), ((0, 1), (1, 0)))
-    errorX = np.zeros(N + 1)
-    errorY = np.zeros(N + 1)
+    # per frame J: row J plus column J-1 (column -1 for J = 0, as Python
+    # indexes it); the column sums run over contiguous copies of the columns,
+    # so every sum adds the same numbers in the same order as np.sum of a row
+    # or column slice
+    prev = np.arange(N + 1) - 1
+
+    def row_col(a):
+        return a.sum(axis=1) + np.ascontiguousarray(a.T).sum(axis=1)[prev]
+
     with np.errstate(all="ignore"):
-        for J in range(N + 1):
-            den = np.sum(wu[J, :]) + np.sum(wu[:, J - 1])
-            errorX[J] = (np.sum(ex[J, :] * wu[J, :]) + np.sum(ex[:, J - 1] * wu[:, J - 1])) / den
-            errorY[J] = (np.sum(ey[J, :] * wu[J, :]) + np.sum(ey[:, J - 1] * wu[:, J - 1])) / den
+        den = row_col(wu)
+        errorX = row_col(ex * wu) / den
+        errorY = row_col(ey * wu) / den
     ed.update({"translations": -np.vstack((np.zeros([1, 2]), np.cumsum(rel, axis=0))), "relativeEst": rel,
                "acceptedEqns": accepted, "weights": weights, "errorXY": errorXY, "shiftsTriMat": shiftsTriMat_in,
                "errorX": errorX, "errorY": errorY, "errorUnraveled": errorUnraveled, "mean_errorNorm": mean_e,
