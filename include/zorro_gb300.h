@@ -141,6 +141,13 @@ int zr_hotpix_maps(const float* unaligned_sum, int height, int width, int n_fram
                    const zr_hotpix_params_t* params, float* hot_a, float* hot_b,
                    unsigned int* counts3, void* work, size_t work_bytes, void* stream);
 
+/* ---- movie input: MRC mode 101 (zorro.loadData, zorro.py:3414-3425, read
+ * through mrcz) ----
+ * frames[n][y][x] (uint8) = 4-bit pixel x of row y of frame n in ``packed``
+ * ([n_frames][height][(width+1)/2] bytes, the first pixel of each byte in its
+ * low 4 bits, rows padded to whole bytes). */
+int zr_unpack_u4(const void* packed, int n_frames, int height, int width, void* frames, void* stream);
+
 /* ---- Fourier binning: binStack(binKernel='fourier'), zorro.py:1826-1904 ----
  * out[n] (float, [Hb][Wb]) = real(IFFT_unscaled(crop(FFT(frame n))) / (Hb Wb)),
  * the crop keeping rows [0, Hb/2) and [H - Hb/2, H) and columns likewise; the

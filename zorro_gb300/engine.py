@@ -152,6 +152,16 @@ class Engine:
     def upload(self, reg):
         torch = self.torch
         imgs = reg.images
+        from .mrc import Packed4
+        if isinstance(imgs, Packed4):
+            # 4-bit movie: the packed bytes cross the host link, the device
+            # expands them into the uint8 frames the kernels read
+            N, H, W = imgs.shape
+            src = torch.from_numpy(np.ascontiguousarray(imgs.data).reshape(-1))
+            packed = self.buf("u4packed", src.numel())[:src.numel()]
+            packed.copy_(src, non_blocking=True)
+            imgs = self.tensor("u4frames", (N, H, W), torch.uint8)
+            self.call("A_gain_sum", "zr_unpack_u4", packed.data_ptr(), N, H, W, imgs.data_ptr(), self.stream)
         if isinstance(imgs, torch.Tensor):
             t = imgs.to(self.dev, non_blocking=True)
             dt = np.dtype(str(t.dtype).replace("torch.", ""))
@@ -167,7 +177,8 @@ class Engine:
             raise ValueError("images dtype %s not supported (float32, uint8, uint16, float16)" % dt)
         t = t.contiguous()
         gain = None
-        if reg.gainRef is not None and dt != np.dtype(np.float32):
+        raw_float = bool(getattr(reg, "imagesAreRaw", False))  # float frames read by loadData, gain not applied
+        if reg.gainRef is not None and (dt != np.dtype(np.float32) or raw_float):
             g = reg.gainRef
             gain = (g.to(self.dev) if isinstance(g, torch.Tensor) else torch.from_numpy(
                 np.ascontiguousarray(g, dtype=np.float32)).to(self.dev, non_blocking=True)).float().contiguous()
@@ -275,7 +286,9 @@ class Engine:
                                  "(zorro.py:895)")
         raw, gain, rtype = self.upload(reg)
         N, H, W = (int(s) for s in raw.shape)
-        gdiv = float(reg.gain) if (reg.gain and not np.isclose(reg.gain, 1.0) and rtype != _lib.ZR_F32) else 0.0
+        raw_float = bool(getattr(reg, "imagesAreRaw", False))
+        gdiv = float(reg.gain) if (reg.gain and not np.isclose(reg.gain, 1.0) and (rtype != _lib.ZR_F32 or raw_float)) \
+            else 0.0
         frames = self._frames(raw, rtype, gain, gdiv=gdiv)
         pixelsize = reg.pixelsize
         if reg.shapeBinned is not None and np.any(reg.shapeBinned):
@@ -625,6 +638,7 @@ class Engine:
             out["filtSum"] = fetch(filt_sum)
         if reg.keepAlignedImages:
             out["images"] = fetch(aligned)
+            out["imagesAreRaw"] = False
         if pending:
             torch.cuda.current_stream(self.dev).synchronize()
             for k in ("imageSum", "FRC", "FRC2D", "filtSum", "images"):

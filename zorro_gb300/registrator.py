@@ -97,10 +97,20 @@ class ImageRegistrator:
         self.diagWidth = 5
         self.autoMax = 10
         self.corrThres = None
+        # input/output (zorro.py:218-230)
+        self.files = {"config": None, "stack": None, "mask": None, "sum": None, "align": None, "figurePath": None,
+                      "xc": None, "moveRawPath": None, "original": None, "gainRef": None, "stdout": None,
+                      "automatch": None, "rejected": None, "compressor": None, "clevel": 1}
+        self.saveMovie = True
+        self.doCompression = False
+        self.compress_ext = ".bz2"
         # GB300 build: options of the GPU path
         self.keepAlignedImages = True   # copy the shifted frames back into ``images``
         self.subtractFrameMean = True    # exact identity, see zorro_gb300.engine
         self.returnDeviceArrays = False  # leave imageSum/filtSum/FRC as CUDA tensors
+        # float32 ``images`` from loadData still without gainRef / gain (the
+        # kernels apply them as they read the frames)
+        self.imagesAreRaw = False
         # 'float16': frame spectra stored in half precision with per-spectrum
         # power-of-two scales (products and transforms stay float32)
         self.spectraPrecision = "float32"
@@ -126,6 +136,99 @@ class ImageRegistrator:
         self.gainRef = np.ascontiguousarray(g)
         return self.gainRef
 
+    def loadData(self, stackNameIn=None, target="stack"):
+        """Read an MRC file into ``target`` (zorro.py:3268-3516, MRC branch
+        :3414-3425 and the gain / assignment steps :3455-3516).
+
+        * The pixel size comes from the header when it is nonzero (nm), for
+          every target: a gain reference read on behalf of a movie replaces
+          the movie's pixel size when its own header has one, as in the
+          reference.
+        * Movies stay in their detector type (uint8, uint16, float16, float32,
+          or the packed 4-bit ``mrc.Packed4``) in page-locked host memory,
+          int8/int16 ones become float32; the gain reference multiply and the
+          ``gain`` division that the reference applies here on the host run
+          inside the kernels that read the frames (same float32 values).
+          ``imagesAreRaw`` marks float32 frames that still need them.
+        * target 'gainRef' orients the reference by ``gainInfo``
+          (``loadGainRef``); 'sum'/'imageSum', 'filt'/'filtSum' and 'mask'
+          set those attributes.
+
+        DM3/DM4/TIFF/HDF5 and compressed files are not read."""
+        import os
+
+        from . import mrc
+        if stackNameIn is not None:
+            self.files[target] = stackNameIn
+        name = self.files.get(target)
+        if not name:
+            raise ValueError("zorro.loadData: no file for target %r" % target)
+        ext = os.path.splitext(str(name))[1].lower()
+        if ext not in (".mrc", ".mrcs"):
+            raise ValueError("zorro.loadData: %s files are not supported (MRC .mrc/.mrcs only)" % ext)
+        data, hdr = mrc.read(name, pinned=target in ("stack", "align", "images"))
+        if not np.isclose(hdr["pixelsize"][0], 0.0):
+            self.pixelsize = np.float32(hdr["pixelsize"][0])
+        if target in ("stack", "align", "images"):
+            if data.ndim != 3 or data.shape[0] < 2:  # a single image, saved by mistake
+                self.METAstatus = "error"
+                raise ValueError("zorro.loadData: stacks must be 3D data")
+            if target != "gainRef" and self.files.get("gainRef") and self.gainRef is None:
+                self.loadData(self.files["gainRef"], target="gainRef")
+            # gainRef and gain are applied as the kernels read the frames
+            if isinstance(data, mrc.Packed4) or data.dtype in (np.uint8, np.uint16, np.float16, np.float32):
+                self.images = data
+            else:
+                self.images = data.astype(np.float32)  # float32(int), as the reference's astype
+            self.imagesAreRaw = not isinstance(data, mrc.Packed4) and self.images.dtype == np.float32
+        elif target == "gainRef":
+            if isinstance(data, mrc.Packed4):
+                raise ValueError("zorro.loadData: a 4-bit gain reference is not supported")
+            self.loadGainRef(data[0] if data.shape[0] == 1 else data)
+        elif target in ("sum", "imageSum"):
+            self.imageSum = np.asarray(data[0] if data.shape[0] == 1 else data, dtype=np.float32)
+        elif target in ("filt", "filtSum"):
+            self.filtSum = np.asarray(data[0] if data.shape[0] == 1 else data, dtype=np.float32)
+        elif target == "mask":
+            self.masks = np.asarray(data)
+        else:
+            raise ValueError("zorro.loadData: unknown target %r" % target)
+
+    def saveData(self):
+        """Write the aligned sum, the aligned movie (``saveMovie``) and the
+        filtered sum as MRC files (zorro.py:3538-3627): default names
+        sum/<stack>_zorro.mrc, align/<stack>_zorro_movie.mrcs and
+        <sum>_filt.mrc next to the sum, pixel size in the header.  Compressed
+        output (``files['compressor']``, ``doCompression``) is not written."""
+        import os
+
+        from . import mrc
+        if self.files.get("compressor") or self.doCompression:
+            raise ValueError("zorro.saveData: compressed output is not supported")
+        stack = self.files.get("stack") or "stack.mrc"
+        front, ext = os.path.splitext(os.path.basename(str(stack)))
+        if ext in (".bz2", ".gz", ".7z"):
+            front = os.path.splitext(front)[0]
+        if self.files.get("sum") is None:
+            self.files["sum"] = os.path.join("sum", "%s_zorro.mrc" % front)
+        sum_path = self.files["sum"]
+        mrc.write(sum_path, self._host(self.imageSum), pixelsize=self.pixelsize)
+        if self.saveMovie and self.images is not None and not isinstance(self.images, mrc.Packed4):
+            if self.files.get("align") is None:
+                self.files["align"] = os.path.join("align", "%s_zorro_movie.mrcs" % front)
+            mrc.write(self.files["align"], self._host(self.images), pixelsize=self.pixelsize)
+        if self.filterMode and self.filtSum is not None:
+            if self.files.get("filt") is None:
+                self.files["filt"] = os.path.join(os.path.dirname(sum_path),
+                                                  "%s_filt.mrc" % os.path.splitext(os.path.basename(sum_path))[0])
+            mrc.write(self.files["filt"], self._host(self.filtSum), pixelsize=self.pixelsize)
+
+    @staticmethod
+    def _host(a):
+        if hasattr(a, "detach"):
+            a = a.detach().cpu().numpy()
+        return np.asarray(a)
+
     def alignImageStack(self):
         """Register and sum the stack.  zorro.py:1569-1716."""
         if str(self.xcorrMode).lower() != "zorro":
@@ -138,7 +241,7 @@ def copy_config(src, dst):
     """Copy the registration attributes of one registrator to another."""
     for k, v in vars(src).items():
         if k in ("images", "imageSum", "filtSum", "gainRef", "masks", "errorDictList", "FRC", "FRC2D",
-                 "translations"):
+                 "translations", "files", "imagesAreRaw"):
             continue
         setattr(dst, k, copy.deepcopy(v))
     return dst
