@@ -15,7 +15,7 @@ from zorro_gb300.synthetic import make_movie
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("shape", [(1, 1, 1), (3, 5, 9), (2, 7, 64), (4, 37, 3710)])
+@pytest.mark.parametrize("shape", [(1, 1, 1), (1, 1, 2), (1, 3, 10), (3, 5, 9), (2, 7, 64), (4, 37, 3710)])
 def test_unpack_u4_matches_oracle(shape):
     import torch
     rng = np.random.default_rng(sum(shape))
