@@ -26,6 +26,7 @@ frames in ``images``; here that happens when ``keepAlignedImages`` is True
 from __future__ import annotations
 
 import copy
+import tempfile
 import time
 
 import numpy as np
@@ -38,16 +39,23 @@ class ImageRegistrator:
     """GPU drop-in for zorro.ImageRegistrator's registration path."""
 
     def __init__(self):
-        # defaults of zorro.py:82-243 that the hot path reads
+        # defaults of zorro.py:82-243 (the hot path's, and the rest of what
+        # the .zor configs carry)
         self.verbose = 0
+        self.umask = 2
+        self.METApriority = 0.0
         self.METAstatus = "new"
+        self.METAmtime = 0.0
+        self.METAsize = 0
         self.xcorrMode = "zorro"
+        self.fftw_effort = "FFTW_MEASURE"
         self.n_threads = None
-        self.cachePath = None
+        self.cachePath = tempfile.gettempdir()
         self.pixelsize = None
         self.voltage = 300.0
         self.C3 = 2.7
         self.gain = None
+        self.detectorPixelSize = None
         self.bench = {}
         self.saveC = False
         self.Brad = 512
@@ -68,7 +76,12 @@ class ImageRegistrator:
         self.masks = None
         self.C = None
         self.translations = None
+        self.velocities = None
+        self.rotations = None
+        self.scales = None
         self.errorDictList = []
+        self.trackCorrStats = False
+        self.corrStats = None
         self.doLazyFRC = True
         self.doEvenOddFRC = False
         self.FRC = None
@@ -76,6 +89,9 @@ class ImageRegistrator:
         self.transEven = None   # half-set trajectories of doEvenOddFRC
         self.transOdd = None
         self.CTFProgram = None
+        self.CTFInfo = {"DefocusU": None, "DefocusV": None, "DefocusAngle": None, "CtfFigureOfMerit": None,
+                        "FinalResolution": None, "AmplitudeContrast": 0.07, "AdditionalPhaseShift": None}
+        self.CTFDiag = None
         self.shapePadded = [4096, 4096]
         self.shapeOriginal = None
         self.shapeBinned = None
@@ -97,13 +113,22 @@ class ImageRegistrator:
         self.diagWidth = 5
         self.autoMax = 10
         self.corrThres = None
+        self.velocityThres = None
         # input/output (zorro.py:218-230)
         self.files = {"config": None, "stack": None, "mask": None, "sum": None, "align": None, "figurePath": None,
                       "xc": None, "moveRawPath": None, "original": None, "gainRef": None, "stdout": None,
                       "automatch": None, "rejected": None, "compressor": None, "clevel": 1}
+        self.savePNG = True
         self.saveMovie = True
         self.doCompression = False
         self.compress_ext = ".bz2"
+        # plotting options (zorro.py:233-241): carried through the configs, no plots are drawn
+        self.plotDict = {"imageSum": True, "imageFirst": False, "FFTSum": True, "polarFFTSum": True, "filtSum": True,
+                         "stats": False, "corrTriMat": False, "peaksigTriMat": True, "translations": True,
+                         "pixRegError": True, "CTFDiag": True, "logisticWeights": True, "FRC": True,
+                         "Transparent": True, "plot_dpi": 144, "image_dpi": 250, "image_cmap": "gray",
+                         "graph_cmap": "gnuplot", "fontsize": 12, "fontstyle": "serif", "colorbar": True,
+                         "backend": "Qt4Agg", "multiprocess": True, "show": False}
         # GB300 build: options of the GPU path
         self.keepAlignedImages = True   # copy the shifted frames back into ``images``
         self.subtractFrameMean = True    # exact identity, see zorro_gb300.engine
@@ -222,6 +247,17 @@ class ImageRegistrator:
                 self.files["filt"] = os.path.join(os.path.dirname(sum_path),
                                                   "%s_filt.mrc" % os.path.splitext(os.path.basename(sum_path))[0])
             mrc.write(self.files["filt"], self._host(self.filtSum), pixelsize=self.pixelsize)
+
+    def saveConfig(self, configNameIn=None):
+        """Write the state as a .zor file (zorro.py:3889-4075; zorro_gb300.config)."""
+        from .config import save_config
+        return save_config(self, configNameIn)
+
+    def loadConfig(self, configNameIn=None, loadData=False):
+        """Read a .zor file into the attributes (zorro.py:3682-3887;
+        zorro_gb300.config), then the movie when ``loadData``."""
+        from .config import load_config
+        return load_config(self, configNameIn, loadData)
 
     @staticmethod
     def _host(a):
