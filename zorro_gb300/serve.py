@@ -90,9 +90,15 @@ class MovieServer:
             self._cv.notify_all()
 
     def _run(self, reg, t_submit):
+        from .mrc import Packed4
         imgs = reg.images
         shape = tuple(imgs.shape)
-        itemsize = imgs.element_size() if hasattr(imgs, "element_size") else np.asarray(imgs).dtype.itemsize
+        if isinstance(imgs, Packed4):
+            itemsize = 1.5  # the packed bytes and the uint8 frames they expand into
+        elif hasattr(imgs, "element_size"):
+            itemsize = imgs.element_size()
+        else:
+            itemsize = np.asarray(imgs).dtype.itemsize
         need = movie_bytes(reg, shape, itemsize)
         slot = self._acquire(need)
         try:
