@@ -255,8 +255,39 @@ int zr_xcorr_refine(const void* G, const void* templates, const float* refine_te
 int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr_peak_params_t* params,
                     zr_peak_result_t* results, void* stream);
 
-/* ---- shift and sum: applyShifts + lazyFouRingCorr sums, zorro.py:1734-1808, 2237-2238 ---- */
+/* ---- preShift peak search on uncropped planes: locatePeak with preShift,
+ * zorro.py:1089-1092 (no crop), 1148-1168 (rolled mask) ----
+ * ``planes`` are n whole C x C correlation planes, ifftshifted (the output of
+ * zr_xcorr_pairs with max_shift = C/2).  The host runs the bounded Brent
+ * search over sigma for every plane of a batch in lock step.
+ *
+ * zr_full_prepare: origin[p] = the plane's value at (C/2, C/2); with
+ * suppress_origin the stencil of zorro.py:1082-1083 replaces it (in place);
+ * mean[p] = the plane's mean afterwards.
+ *
+ * zr_full_filter: for the planes listed in sel[0..n_sel), the separable
+ * Gaussian filter (axis 0, then axis 1, 'reflect' borders) with the taps
+ * weights[p][a][0 .. 2*radius[p][a]] of axis a (radius <= 64; 2 x 129 floats
+ * a plane), kept in filtered[p] when ``filtered`` is not NULL; stats[p] =
+ * (sum (F - mean[p]), sum (F - mean[p])^2, max F), summed in a fixed order.
+ *
+ * zr_full_peaks: for the listed planes, the maxShift disc about (C/2, C/2)
+ * np.roll-ed by rolls[p] = (ry, rx): argmax of filtered * disc (first index
+ * on ties), the peak significance over the disc, and the sub-pixel step of
+ * zr_locate_peaks on the filtered plane (unfiltered value at the integer
+ * fallback); results[p] gets sigma[p] and nfev[p] as given.
+ * work: zr_full_work_bytes(n_planes, C) bytes. */
+int zr_full_prepare(float* planes, int n, int C, int suppress_origin, float* origin, float* mean, void* stream);
+size_t zr_full_work_bytes(int n_planes, int C);
+int zr_full_filter(const float* planes, int n_planes, int C, const int* sel, int n_sel, const float* weights,
+                   const int* radius, const float* mean, float* filtered, double* stats, void* work,
+                   size_t work_bytes, void* stream);
+int zr_full_peaks(const float* planes, const float* filtered, int n_planes, int C, const int* sel, int n_sel,
+                  int max_shift, const int* rolls, const float* mean, const float* origin, const double* sigma,
+                  const int* nfev, int sub_pix_reg, zr_peak_result_t* results, void* work, size_t work_bytes,
+                  void* stream);
 
+/* ---- shift and sum: applyShifts + lazyFouRingCorr sums, zorro.py:1734-1808, 2237-2238 ---- */
 /* image_sum = sum_n shifted frame n (float32, frame order); even_sum/odd_sum
  * likewise over even/odd n (either may be NULL); ``aligned`` [N][H][W]
  * receives the shifted frames when not NULL.  shifts: device array [N]. */

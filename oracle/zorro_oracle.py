@@ -185,9 +185,10 @@ def opti_sigma(C):
     return float(res.x), scipy.ndimage.gaussian_filter(C, res.x)
 
 
-def locate_peak(C, mask_maxShift, subPixReg=16, Bmode="opti", Brad=512, shapePadded=None, dt=None):
+def locate_peak(C, mask_maxShift, subPixReg=16, Bmode="opti", Brad=512, shapePadded=None, dt=None, roll=None):
     """Peak position with Fourier-interpolated sub-pixel refinement.
-    zorro.py:1099-1231 (preShift=False branch).
+    zorro.py:1099-1231.  With ``roll`` (preShift, zorro.py:1148-1162) the
+    search mask is np.roll-ed by (roll[0], roll[1]) first.
 
     Returns dict(shift[2], corr, peaksig, sigma, C_filt)."""
     sigma = None
@@ -199,6 +200,8 @@ def locate_peak(C, mask_maxShift, subPixReg=16, Bmode="opti", Brad=512, shapePad
     else:
         C_filt = C
     subR = 8
+    if mask_maxShift is not None and roll is not None:
+        mask_maxShift = np.roll(np.roll(mask_maxShift, int(roll[0]), axis=0), int(roll[1]), axis=1)
     if mask_maxShift is not None:
         C_masked = C_filt * mask_maxShift
         cmaxpos = np.unravel_index(np.argmax(C_masked), C_filt.shape)
@@ -232,14 +235,28 @@ def locate_peak(C, mask_maxShift, subPixReg=16, Bmode="opti", Brad=512, shapePad
             "C_filt": C_filt, "cmaxpos": cmaxpos}
 
 
+def preshift_mask(sC, maxShift):
+    """The search mask of preShift: the whole cropped grid, radius maxShift
+    about its centre.  zorro.py:841-851 (preShift branch)."""
+    c2 = (np.array(sC) / 2.0).astype(int)
+    xmesh, ymesh = np.meshgrid(np.arange(-c2[0], c2[0]), np.arange(-c2[1], c2[1]))
+    return (xmesh * xmesh + ymesh * ymesh) < maxShift ** 2.0
+
+
 def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diagWidth=5, diagStart=0,
               maxShift=100, subPixReg=16, Bmode="opti", Brad=512, suppressOrigin=True, dt=None,
-              capture=None, pairs_limit=None):
-    """All-pairs registration.  zorro.py:773-1011 (single mask, preShift
-    off).  triMode 'refine' (zorro.py:934-954) correlates each frame I < N-1
-    with the template conj(sum_n G_n - G_I) / N (and likewise for the squared
-    spectra), filling the diagonal.  Returns (shiftsTriMat, corrTriMat,
-    peaksigTriMat, originTriMat)."""
+              capture=None, pairs_limit=None, preShift=False, peaksigThres=6.0, autoMax=10):
+    """All-pairs registration.  zorro.py:773-1011 (single mask).  triMode
+    'refine' (zorro.py:934-954) correlates each frame I < N-1 with the
+    template conj(sum_n G_n - G_I) / N (and likewise for the squared
+    spectra), filling the diagonal.  With ``preShift`` (zorro.py:1089-1092,
+    1148-1162) the correlation planes are not cropped and the maxShift disc
+    is rolled by the rounded shift of the previous pair of the row,
+    shiftsTriMat[I, J-1] ('refine': shiftsTriMat[I-1, I-1]), as measured so
+    far in cropped pixels.  triMode 'auto' stops a row after the first pair
+    whose peak significance is <= peaksigThres or whose J - I >= autoMax
+    (zorro.py:995-997).  Returns (shiftsTriMat, corrTriMat, peaksigTriMat,
+    originTriMat)."""
     N = images_padded.shape[0]
     tri = tri_indices(N, triMode, diagWidth, diagStart)
     if np.any(fouCrop):
@@ -248,7 +265,9 @@ def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diag
         sC = np.array(images_padded.shape[1:])
     nc2 = norm_const2(sC)
     GM, MP = mask_spectrum(mask, sC, dt)
-    mmask = max_shift_mask(maxShift) if maxShift else None
+    pre = bool(preShift) and bool(maxShift)
+    mmask = (preshift_mask(sC, maxShift) if pre else max_shift_mask(maxShift)) if maxShift else None
+    crop = None if pre else maxShift
     G = [None] * N
     S = [None] * N
     for I in range(N):
@@ -264,10 +283,11 @@ def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diag
         for I in range(N - 1):
             # mnxc2 conjugates its template argument: conj((sum - G_I) / N)
             # equals the reference's conj(sum - G_I) / N exactly
-            C, o = mnxc2((sumG - G[I]) / N, (sumS - S[I]) / N, G[I], S[I], GM, MP, nc2, maxShift, suppressOrigin,
+            C, o = mnxc2((sumG - G[I]) / N, (sumS - S[I]) / N, G[I], S[I], GM, MP, nc2, crop, suppressOrigin,
                          dt)
             origin[I, I] = o
-            r = locate_peak(C, mmask, subPixReg, Bmode, Brad, shapePadded, dt)
+            roll = np.round(shifts[I - 1, I - 1]).astype(int) if pre else None
+            r = locate_peak(C, mmask, subPixReg, Bmode, Brad, shapePadded, dt, roll=roll)
             shifts[I, I, :] = r["shift"]
             corr[I, I] = r["corr"]
             peaksig[I, I] = r["peaksig"]
@@ -276,9 +296,10 @@ def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diag
     pair_rows = [] if triMode == "refine" else np.unique(np.argwhere(np.sum(tri, axis=1) > 0))
     for I in pair_rows:
         for J in np.unique(np.argwhere(tri[I, :])):
-            C, o = mnxc2(G[I], S[I], G[J], S[J], GM, MP, nc2, maxShift, suppressOrigin, dt)
+            C, o = mnxc2(G[I], S[I], G[J], S[J], GM, MP, nc2, crop, suppressOrigin, dt)
             origin[I, J] = o
-            r = locate_peak(C, mmask, subPixReg, Bmode, Brad, shapePadded, dt)
+            roll = np.round(shifts[I, J - 1]).astype(int) if pre else None
+            r = locate_peak(C, mmask, subPixReg, Bmode, Brad, shapePadded, dt, roll=roll)
             shifts[I, J, :] = r["shift"]
             corr[I, J] = r["corr"]
             peaksig[I, J] = r["peaksig"]
@@ -286,6 +307,8 @@ def xcorr_tri(images_padded, mask, *, shapePadded, fouCrop, triMode="diag", diag
                 capture[(int(I), int(J))] = {"C": C, "sigma": r["sigma"], "C_filt": r["C_filt"]}
             done += 1
             if pairs_limit is not None and done >= pairs_limit:
+                break
+            if triMode == "auto" and (peaksig[I, J] <= peaksigThres or J - I >= autoMax):
                 break
         if pairs_limit is not None and done >= pairs_limit:
             break
@@ -763,7 +786,7 @@ def hotpix_filter(images, hotpixInfo, neighbourThres=0.01, dt=None):
 # --------------------------------------------------------------------------
 
 DEFAULTS = dict(shapeBinned=None, shapePadded=[4096, 4096], fouCrop=[3072, 3072], triMode="diag", diagWidth=5, diagStart=0,
-                maxShift=100, subPixReg=16, Bmode="opti", Brad=512, weightMode="autologistic",
+                maxShift=100, preShift=False, autoMax=10, subPixReg=16, Bmode="opti", Brad=512, weightMode="autologistic",
                 peaksigThres=6.0, logisticK=5.0, logisticNu=0.15, originMode="centroid",
                 suppressOrigin=True, shiftMethod="lanczos", doLazyFRC=True, doEvenOddFRC=False, filterMode=None,
                 doseFiltParam=[None, 0.24499, -1.6649, 2.8141, 32, 0], pixelsize=None, voltage=300.0,
@@ -839,7 +862,9 @@ def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
     sh, co, ps, orig = xcorr_tri(padded, mask, shapePadded=P, fouCrop=o["fouCrop"], triMode=o["triMode"],
                                  diagWidth=o["diagWidth"], diagStart=o["diagStart"], maxShift=o["maxShift"],
                                  subPixReg=o["subPixReg"], Bmode=o["Bmode"], Brad=o["Brad"],
-                                 suppressOrigin=o["suppressOrigin"], dt=dt, capture=capture)
+                                 suppressOrigin=o["suppressOrigin"], dt=dt, capture=capture,
+                                 preShift=o.get("preShift", False), peaksigThres=o["peaksigThres"],
+                                 autoMax=o.get("autoMax", 10))
     bench["xcorr3"] = time.time()
     if o["triMode"] == "first":
         translations = -sh[0, :]

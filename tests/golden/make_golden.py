@@ -60,6 +60,15 @@ CASES = {
     "refine_mode": dict(movie=dict(n_frames=10, shape=(200, 180), seed=12, mean_dose=1.5, drift_sigma=0.8),
                         attrs=dict(triMode="refine", shapePadded=[256, 256], fouCrop=[128, 128], maxShift=20,
                                    pixelsize=0.1, doLazyFRC=False)),
+    # preShift: uncropped correlation planes, the maxShift disc rolled to the
+    # previous pair of each row (a drift larger than the disc over the row)
+    "preshift": dict(movie=dict(n_frames=8, shape=(120, 128), seed=23, mean_dose=3.0, drift_sigma=2.5),
+                     attrs=dict(triMode="tri", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=8,
+                                pixelsize=0.1, preShift=True, doLazyFRC=False)),
+    # auto mode: each row stops at the first weak pair or at autoMax frames
+    "auto_mode": dict(movie=dict(n_frames=14, shape=(200, 180), seed=29, mean_dose=1.2, drift_sigma=0.8),
+                      attrs=dict(triMode="auto", autoMax=6, peaksigThres=5.6, shapePadded=[256, 256],
+                                 fouCrop=[128, 128], maxShift=20, pixelsize=0.1, doLazyFRC=False)),
     # template mode: correlate everything to frame 0, no solver
     "first_mode": dict(movie=dict(n_frames=5, shape=(120, 128), seed=21, mean_dose=3.0, drift_sigma=1.0),
                        attrs=dict(triMode="first", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=16,

@@ -21,7 +21,7 @@ EXPORTS = (
     "zr_shift_sum", "zr_frc_work_bytes", "zr_tiled_frc", "zr_dose_work_bytes", "zr_dose_filter",
     "zr_l1_solve", "zr_xcorr_pairs_noalloc", "zr_logistic_fit", "zr_refine_spectra", "zr_refine_terms",
     "zr_xcorr_refine", "zr_pack_half", "zr_xcorr_terms_half", "zr_xcorr_pairs_half", "zr_bin_work_bytes",
-    "zr_bin_fourier", "zr_unpack_u4",
+    "zr_bin_fourier", "zr_unpack_u4", "zr_full_prepare", "zr_full_work_bytes", "zr_full_filter", "zr_full_peaks",
 )
 
 
@@ -90,6 +90,11 @@ _SIGS = {
     "zr_bin_work_bytes": (C.c_size_t, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "zr_bin_fourier": (C.c_int, [C.POINTER(Frames), C.c_int, C.c_int, _P, _P, C.c_size_t, _P]),
     "zr_unpack_u4": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "zr_full_prepare": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P, _P]),
+    "zr_full_work_bytes": (C.c_size_t, [C.c_int, C.c_int]),
+    "zr_full_filter": (C.c_int, [_P, C.c_int, C.c_int, _P, C.c_int, _P, _P, _P, _P, _P, _P, C.c_size_t, _P]),
+    "zr_full_peaks": (C.c_int, [_P, _P, C.c_int, C.c_int, _P, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P, _P,
+                                C.c_size_t, _P]),
     "zr_pack_half": (C.c_int, [_P, C.c_int, C.c_longlong, _P, _P, _P, C.c_size_t, _P]),
     "zr_xcorr_terms_half": (C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P, C.c_size_t, _P]),
     "zr_xcorr_pairs_half": (C.c_int, [_P, _P, _P, _P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P,

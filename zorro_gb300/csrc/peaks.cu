@@ -480,6 +480,70 @@ __device__ float filtered_at(const float* C, int w, int y, int x, int ry, int rx
   return f;
 }
 
+// The sub-pixel step on a 16 x 16 filtered patch (zorro.py:1180-1216): its
+// forward DFT (rows, then columns), the inverse DFT upsampled to an L x L
+// grid (L = 16*sp, frequencies -8..7, unscaled like the reference's
+// subIFFT2.execute()), |.| and its argmax (first index on ties).  ``scratch``
+// holds 17*L float2 of shared memory.  All threads call.
+__device__ void subpix_search(const float* patch, int sp, const float2* __restrict__ tw, float2* scratch,
+                              float2* patchF, PkShared& sh, float& bv, int& bi) {
+  __shared__ float2 rowF[16 * 16];
+  for (int e = threadIdx.x; e < 256; e += PK_T) {
+    const int i = e >> 4, v = e & 15;
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (int j = 0; j < 16; j++) {
+      const float2 t = __ldg(tw + ((v * j) & 15) * (TWN / 16));
+      acc.x = fmaf(patch[i * 16 + j], t.x, acc.x);
+      acc.y = fmaf(patch[i * 16 + j], t.y, acc.y);
+    }
+    rowF[e] = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 256; e += PK_T) {
+    const int u = e >> 4, v = e & 15;
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (int i = 0; i < 16; i++) acc = cadd(acc, cmul(rowF[i * 16 + v], __ldg(tw + ((u * i) & 15) * (TWN / 16))));
+    patchF[e] = acc;
+  }
+  __syncthreads();
+  // exp(+2 pi i m / L) for m in [0, L), after the L x 16 intermediate
+  const int L = 16 * sp;
+  const int tws = TWN / L;
+  float2* Tx = scratch;
+  float2* Wl = Tx + 16 * L;
+  for (int m = threadIdx.x; m < L; m += PK_T) {
+    float2 t = __ldg(tw + m * tws);
+    t.y = -t.y;
+    Wl[m] = t;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 16 * L; e += PK_T) {
+    const int fyi = e / L, nx = e - fyi * L;
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (int fxi = 0; fxi < 16; fxi++) {
+      const int fx = fxi - 8;
+      const float2 t = Wl[(fx * nx) & (L - 1)];
+      acc = cadd(acc, cmul(patchF[((fyi - 8) & 15) * 16 + (fx & 15)], t));
+    }
+    Tx[fyi * L + nx] = acc;
+  }
+  __syncthreads();
+  bv = -INFINITY;
+  bi = 0x7fffffff;
+  for (int e = threadIdx.x; e < L * L; e += PK_T) {
+    const int ny = e / L, nx = e - ny * L;
+    float2 acc = make_float2(0.0f, 0.0f);
+    for (int fyi = 0; fyi < 16; fyi++) {
+      const int fy = fyi - 8;
+      const float2 t = Wl[(fy * ny) & (L - 1)];
+      acc = cadd(acc, cmul(Tx[fyi * L + nx], t));
+    }
+    const float mag = sqrtf(acc.x * acc.x + acc.y * acc.y);
+    if (mag > bv || (mag == bv && e < bi)) { bv = mag; bi = e; }
+  }
+  block_argmax(sh, bv, bi);
+}
+
 __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwin, int mS, zr_peak_params_t p,
                                                zr_peak_result_t* __restrict__ res, const float2* __restrict__ tw) {
   extern __shared__ float smf[];
@@ -555,67 +619,10 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
         patch[e] = filtered_at(C, w, cy - PK_SUBR + i, cx - PK_SUBR + j, ry, rx, sh.wy, sh.wx);
       }
       __syncthreads();
-      // row DFTs then column DFTs (16-point, twiddles from the 8192 table)
-      __shared__ float2 rowF[16 * 16];
-      for (int e = threadIdx.x; e < 256; e += PK_T) {
-        const int i = e >> 4, v = e & 15;
-        float2 acc = make_float2(0.0f, 0.0f);
-        for (int j = 0; j < 16; j++) {
-          const float2 t = __ldg(tw + ((v * j) & 15) * (TWN / 16));
-          acc.x = fmaf(patch[i * 16 + j], t.x, acc.x);
-          acc.y = fmaf(patch[i * 16 + j], t.y, acc.y);
-        }
-        rowF[e] = acc;
-      }
-      __syncthreads();
-      for (int e = threadIdx.x; e < 256; e += PK_T) {
-        const int u = e >> 4, v = e & 15;
-        float2 acc = make_float2(0.0f, 0.0f);
-        for (int i = 0; i < 16; i++) acc = cadd(acc, cmul(rowF[i * 16 + v], __ldg(tw + ((u * i) & 15) * (TWN / 16))));
-        patchF[e] = acc;
-      }
-      __syncthreads();
-      // Upsampled inverse DFT on an L x L grid, L = 16*sp: frequencies -8..7.
-      // exp(+2 pi i m / L) for m in [0, L) is staged in shared memory after
-      // the L x 16 intermediate.
       const int L = 16 * sp;
-      const int tws = TWN / L;
-      float2* Tx = (float2*)C;  // the window is no longer needed
-      float2* Wl = Tx + 16 * L;
-      __syncthreads();
-      for (int m = threadIdx.x; m < L; m += PK_T) {
-        float2 t = __ldg(tw + m * tws);
-        t.y = -t.y;
-        Wl[m] = t;
-      }
-      __syncthreads();
-      for (int e = threadIdx.x; e < 16 * L; e += PK_T) {
-        const int fyi = e / L, nx = e - fyi * L;
-        float2 acc = make_float2(0.0f, 0.0f);
-        for (int fxi = 0; fxi < 16; fxi++) {
-          const int fx = fxi - 8;
-          const float2 t = Wl[(fx * nx) & (L - 1)];
-          acc = cadd(acc, cmul(patchF[((fyi - 8) & 15) * 16 + (fx & 15)], t));
-        }
-        Tx[fyi * L + nx] = acc;
-      }
-      __syncthreads();
-      // |.| of the unscaled inverse (the reference's subIFFT2.execute(),
-      // zorro.py:1199), so corr = max / 16^2 carries its scale
-      float bv = -INFINITY;
-      int bi = 0x7fffffff;
-      for (int e = threadIdx.x; e < L * L; e += PK_T) {
-        const int ny = e / L, nx = e - ny * L;
-        float2 acc = make_float2(0.0f, 0.0f);
-        for (int fyi = 0; fyi < 16; fyi++) {
-          const int fy = fyi - 8;
-          const float2 t = Wl[(fy * ny) & (L - 1)];
-          acc = cadd(acc, cmul(Tx[fyi * L + nx], t));
-        }
-        const float mag = sqrtf(acc.x * acc.x + acc.y * acc.y);
-        if (mag > bv || (mag == bv && e < bi)) { bv = mag; bi = e; }
-      }
-      block_argmax(sh, bv, bi);
+      float bv;
+      int bi;
+      subpix_search(patch, sp, tw, (float2*)C, patchF, sh, bv, bi);  // the window is no longer needed
       const int sy = bi / L, sx = bi - (bi / L) * L;
       const double ry0 = (double)cy - w / 2.0, rx0 = (double)cx - w / 2.0;
       shy = ry0 + ((double)sy - L / 2.0 + (ry0 > 0 ? 1.0 : (ry0 < 0 ? -1.0 : 0.0))) / sp;
@@ -640,6 +647,316 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
     res[blockIdx.x] = r;
   }
 }
+
+// ---------------------------------------------------------------------------
+// Peak search on uncropped correlation planes (preShift, zorro.py:1089-1092
+// and 1148-1168): each plane is the whole C x C correlation, ifftshifted.  The
+// planes are too large for one CTA, so the steps are separate launches over a
+// batch of planes, driven by the bounded Brent search that the host runs for
+// every plane of the batch in lock step:
+//   k_full_prepare   origin value, the suppressOrigin stencil, plane mean;
+//   k_full_vert      axis-0 Gaussian pass (reflect), into a scratch plane;
+//   k_full_horz      axis-1 pass, its value kept or not, per-CTA partial
+//                    (sum (f - c), sum (f - c)^2, max f) of the statistic;
+//   k_full_reduce    the partials in a fixed order (repeatable sums);
+//   k_full_masked    the maxShift disc rolled by the plane's offset: masked
+//                    argmax (first index on ties) and the partial sums over
+//                    the disc for the peak significance;
+//   k_full_finish    the reduction of those and the sub-pixel step.
+// ``sel`` lists the planes a launch works on (grid z).
+
+constexpr int FP_T = 256;   // threads of the filter and masked passes
+constexpr int FP_TX = 32;   // columns per filter CTA
+constexpr int FP_RY = 64;   // rows per filter CTA
+
+__global__ void __launch_bounds__(1024) k_full_prepare(float* __restrict__ planes, int C, int suppress,
+                                                       float* __restrict__ origin, float* __restrict__ mean) {
+  __shared__ double red[32];
+  float* P = planes + (size_t)blockIdx.x * C * C;
+  const int o = (C / 2) * C + C / 2;
+  if (threadIdx.x == 0) {
+    origin[blockIdx.x] = P[o];
+    if (suppress) {  // literal stencil of zorro.py:1082-1083 at the shifted origin
+      float sm = P[o + C] + P[o + 1];
+      sm = sm + P[o - C];
+      sm = sm + P[o - C];
+      sm = sm + P[o + C + 1];
+      sm = sm + P[o - C + 1];
+      sm = sm + P[o - C + 1];
+      sm = sm + P[o - C - 1];
+      P[o] = 0.125f * sm;
+    }
+  }
+  __syncthreads();
+  float ls = 0.0f;
+  double ds = 0.0;
+  int cnt = 0;
+  for (long long e = threadIdx.x; e < (long long)C * C; e += blockDim.x) {
+    ls += P[e];
+    if (++cnt == 64) { ds += ls; ls = 0.0f; cnt = 0; }
+  }
+  ds += ls;
+  for (int off = 16; off > 0; off >>= 1) ds += __shfl_down_sync(0xffffffffu, ds, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ds;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += red[i];
+    mean[blockIdx.x] = (float)(t / ((double)C * C));
+  }
+}
+
+// T[y][x] = sum_k wy[k] P[reflect(y + k - r)][x], the taps in order
+__global__ void __launch_bounds__(FP_T) k_full_vert(const float* __restrict__ planes, int C, const int* __restrict__ sel,
+                                                  const float* __restrict__ wts, const int* __restrict__ rad,
+                                                  float* __restrict__ tmp) {
+  const int j = blockIdx.z, p = sel[j];
+  const int r = rad[2 * p];
+  const float* w = wts + (size_t)p * 2 * (2 * PK_MAXR + 1);
+  const float* P = planes + (size_t)p * C * C;
+  float* T = tmp + (size_t)j * C * C;
+  const int x = blockIdx.x * FP_TX + (threadIdx.x & (FP_TX - 1));
+  if (x >= C) return;
+  for (int y = blockIdx.y * FP_RY + threadIdx.x / FP_TX; y < min(C, (int)(blockIdx.y + 1) * FP_RY);
+       y += FP_T / FP_TX) {
+    float acc;
+    if (r == 0) {
+      acc = P[(size_t)y * C + x] * w[0];
+    } else {
+      acc = 0.0f;
+      for (int k = 0; k <= 2 * r; k++) acc = fmaf(w[k], __ldg(P + (size_t)reflect_idx(y + k - r, C) * C + x), acc);
+    }
+    T[(size_t)y * C + x] = acc;
+  }
+}
+
+// F[y][x] = sum_k wx[k] T[y][reflect(x + k - r)]; F kept when ``out`` is set;
+// per-CTA partials of sum (F - c), sum (F - c)^2 and max F
+__global__ void __launch_bounds__(FP_T) k_full_horz(const float* __restrict__ tmp, int C, const int* __restrict__ sel,
+                                                  const float* __restrict__ wts, const int* __restrict__ rad,
+                                                  const float* __restrict__ mean, float* __restrict__ out,
+                                                  double* __restrict__ part) {
+  __shared__ double red[FP_T / 32][3];
+  const int j = blockIdx.z, p = sel[j];
+  const int r = rad[2 * p + 1];
+  const float* w = wts + (size_t)p * 2 * (2 * PK_MAXR + 1) + (2 * PK_MAXR + 1);
+  const float* T = tmp + (size_t)j * C * C;
+  const float c = mean[p];
+  const int x = blockIdx.x * FP_TX + (threadIdx.x & (FP_TX - 1));
+  float s1 = 0.0f, s2 = 0.0f, mx = -INFINITY;
+  if (x < C) {
+    for (int y = blockIdx.y * FP_RY + threadIdx.x / FP_TX; y < min(C, (int)(blockIdx.y + 1) * FP_RY);
+         y += FP_T / FP_TX) {
+      const float* row = T + (size_t)y * C;
+      float f;
+      if (r == 0) {
+        f = row[x] * w[0];
+      } else {
+        f = 0.0f;
+        for (int k = 0; k <= 2 * r; k++) f = fmaf(w[k], __ldg(row + reflect_idx(x + k - r, C)), f);
+      }
+      if (out) out[(size_t)p * C * C + (size_t)y * C + x] = f;
+      const float d = f - c;
+      s1 += d;
+      s2 = fmaf(d, d, s2);
+      mx = fmaxf(mx, f);
+    }
+  }
+  double a = s1, b = s2, m = mx;
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, off);
+    b += __shfl_down_sync(0xffffffffu, b, off);
+    m = fmax(m, __shfl_down_sync(0xffffffffu, m, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5][0] = a;
+    red[threadIdx.x >> 5][1] = b;
+    red[threadIdx.x >> 5][2] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0, tm = -INFINITY;
+    for (int i = 0; i < FP_T / 32; i++) {
+      ta += red[i][0];
+      tb += red[i][1];
+      tm = fmax(tm, red[i][2]);
+    }
+    double* q = part + ((size_t)p * gridDim.y * gridDim.x + (size_t)blockIdx.y * gridDim.x + blockIdx.x) * 3;
+    q[0] = ta;
+    q[1] = tb;
+    q[2] = tm;
+  }
+}
+
+// stats[p] = (sum, sum of squares, max) over the partials of plane p, in order
+__global__ void k_full_reduce(const double* __restrict__ part, int nblk, const int* __restrict__ sel,
+                              double* __restrict__ stats) {
+  const int p = sel[blockIdx.x];
+  if (threadIdx.x != 0) return;
+  double a = 0.0, b = 0.0, m = -INFINITY;
+  const double* q = part + (size_t)p * nblk * 3;
+  for (int i = 0; i < nblk; i++) {
+    a += q[3 * i];
+    b += q[3 * i + 1];
+    m = fmax(m, q[3 * i + 2]);
+  }
+  stats[3 * p] = a;
+  stats[3 * p + 1] = b;
+  stats[3 * p + 2] = m;
+}
+
+constexpr int FP_MBLK = 128;  // CTAs per plane of the masked pass
+
+// The disc of radius mS about the plane centre, np.roll-ed by (ry, rx)
+// (zorro.py:1150-1153): pixel (y, x) is in it when the unrolled pixel
+// ((y - ry) mod C, (x - rx) mod C) lies within mS of (C/2, C/2).
+__device__ __forceinline__ bool in_rolled_disc(int y, int x, int C, int mS, int ry, int rx) {
+  int yy = (y - ry) % C, xx = (x - rx) % C;
+  if (yy < 0) yy += C;
+  if (xx < 0) xx += C;
+  const long long dy = yy - C / 2, dx = xx - C / 2;
+  return dy * dy + dx * dx < (long long)mS * mS;
+}
+
+// Per-CTA partials over its share of plane p: the argmax of F * disc (zeros
+// outside the disc compete, first index on ties) and sum (F - c),
+// sum (F - c)^2 and the count over the disc.
+__global__ void __launch_bounds__(FP_T) k_full_masked(const float* __restrict__ filt, int C, const int* __restrict__ sel,
+                                                    int mS, const int* __restrict__ rolls,
+                                                    const float* __restrict__ mean, double* __restrict__ part) {
+  __shared__ float rv[FP_T / 32];
+  __shared__ int ri[FP_T / 32];
+  __shared__ double rs[FP_T / 32][3];
+  const int p = sel[blockIdx.z];
+  const float* F = filt + (size_t)p * C * C;
+  const float c = mean[p];
+  const int ry = rolls[2 * p], rx = rolls[2 * p + 1];
+  float bv = -INFINITY, s1 = 0.0f, s2 = 0.0f;
+  int bi = 0x7fffffff, cnt = 0;
+  const long long n = (long long)C * C;
+  for (long long e = (long long)blockIdx.x * FP_T + threadIdx.x; e < n; e += (long long)gridDim.x * FP_T) {
+    const int y = (int)(e / C), x = (int)(e - (long long)y * C);
+    const float f = F[e];
+    const bool in = in_rolled_disc(y, x, C, mS, ry, rx);
+    const float mv = in ? f : 0.0f;
+    if (mv > bv || (mv == bv && (int)e < bi)) { bv = mv; bi = (int)e; }
+    if (in) {
+      const float d = f - c;
+      s1 += d;
+      s2 = fmaf(d, d, s2);
+      cnt++;
+    }
+  }
+  double a = s1, b = s2, k = cnt;
+  for (int off = 16; off > 0; off >>= 1) {
+    const float ov = __shfl_down_sync(0xffffffffu, bv, off);
+    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+    if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    a += __shfl_down_sync(0xffffffffu, a, off);
+    b += __shfl_down_sync(0xffffffffu, b, off);
+    k += __shfl_down_sync(0xffffffffu, k, off);
+  }
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    rv[wid] = bv;
+    ri[wid] = bi;
+    rs[wid][0] = a;
+    rs[wid][1] = b;
+    rs[wid][2] = k;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < FP_T / 32; i++) {
+      if (rv[i] > rv[0] || (rv[i] == rv[0] && ri[i] < ri[0])) { rv[0] = rv[i]; ri[0] = ri[i]; }
+      rs[0][0] += rs[i][0];
+      rs[0][1] += rs[i][1];
+      rs[0][2] += rs[i][2];
+    }
+    double* q = part + ((size_t)p * gridDim.x + blockIdx.x) * 5;
+    q[0] = rv[0];
+    q[1] = ri[0];
+    q[2] = rs[0][0];
+    q[3] = rs[0][1];
+    q[4] = rs[0][2];
+  }
+}
+
+// One CTA per plane: the masked partials in order, the peak significance,
+// then the sub-pixel step on the filtered plane (or the integer fallback at
+// the plane's edge) as k_peaks does it.
+__global__ void __launch_bounds__(PK_T, 1) k_full_finish(const float* __restrict__ planes,
+                                                       const float* __restrict__ filt, int C,
+                                                       const int* __restrict__ sel, const double* __restrict__ part,
+                                                       const float* __restrict__ mean, const float* __restrict__ origin,
+                                                       const double* __restrict__ sigma, const int* __restrict__ nfev,
+                                                       int sp, zr_peak_result_t* __restrict__ res,
+                                                       const float2* __restrict__ tw) {
+  extern __shared__ float2 scratch[];
+  __shared__ PkShared sh;
+  __shared__ float2 patchF[16 * 16];
+  __shared__ float patch[16 * 16];
+  __shared__ double fin[4];
+  __shared__ int fidx;
+  const int p = sel[blockIdx.x];
+  if (threadIdx.x == 0) {
+    const double* q = part + (size_t)p * FP_MBLK * 5;
+    double bv = q[0], s1 = q[2], s2 = q[3], cnt = q[4];
+    int bi = (int)q[1];
+    for (int i = 1; i < FP_MBLK; i++) {
+      const double* r = q + 5 * i;
+      if (r[0] > bv || (r[0] == bv && (int)r[1] < bi)) { bv = r[0]; bi = (int)r[1]; }
+      s1 += r[2];
+      s2 += r[3];
+      cnt += r[4];
+    }
+    const double m1 = s1 / cnt;
+    const double var = s2 / cnt - m1 * m1;
+    fin[0] = ((double)(float)bv - ((double)mean[p] + m1)) / sqrt(var > 0.0 ? var : 0.0);
+    fin[1] = bv;
+    fidx = bi;
+  }
+  __syncthreads();
+  const int cy = fidx / C, cx = fidx - (fidx / C) * C;
+  const float* P = planes + (size_t)p * C * C;
+  const float* F = filt + (size_t)p * C * C;
+  double shy = (double)cy - C / 2.0, shx = (double)cx - C / 2.0;
+  float corr = P[(size_t)cy * C + cx];
+  int flags = 0;
+  if (sp > 1) {
+    if (cy - PK_SUBR >= 0 && cy + PK_SUBR <= C && cx - PK_SUBR >= 0 && cx + PK_SUBR <= C) {
+      for (int e = threadIdx.x; e < 256; e += PK_T)
+        patch[e] = F[(size_t)(cy - PK_SUBR + (e >> 4)) * C + cx - PK_SUBR + (e & 15)];
+      __syncthreads();
+      const int L = 16 * sp;
+      float bv;
+      int bi;
+      subpix_search(patch, sp, tw, scratch, patchF, sh, bv, bi);
+      const int sy = bi / L, sx = bi - (bi / L) * L;
+      const double ry0 = (double)cy - C / 2.0, rx0 = (double)cx - C / 2.0;
+      shy = ry0 + ((double)sy - L / 2.0 + (ry0 > 0 ? 1.0 : (ry0 < 0 ? -1.0 : 0.0))) / sp;
+      shx = rx0 + ((double)sx - L / 2.0 + (rx0 > 0 ? 1.0 : (rx0 < 0 ? -1.0 : 0.0))) / sp;
+      corr = (float)((double)bv / 256.0);
+    } else {
+      flags |= 1;
+    }
+  }
+  if (threadIdx.x == 0) {
+    zr_peak_result_t r;
+    r.shift_y = shy;
+    r.shift_x = shx;
+    r.sigma = sigma[p];
+    r.corr = corr;
+    r.peaksig = (float)fin[0];
+    r.origin = origin[p];
+    r.cy = cy;
+    r.cx = cx;
+    r.flags = flags;
+    r.nfev = nfev[p];
+    res[p] = r;
+  }
+}
+
+static int full_blocks(int C) { return ((C + FP_TX - 1) / FP_TX) * ((C + FP_RY - 1) / FP_RY); }
 
 }  // namespace zr
 
@@ -672,4 +989,66 @@ extern "C" int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr
                     "k_peaks attr"));
   k_peaks<<<M, PK_T, smem, (cudaStream_t)stream>>>(cwin, max_shift, *params, results, tw);
   return launched("k_peaks");
+}
+
+extern "C" int zr_full_prepare(float* planes, int n, int C, int suppress_origin, float* origin, float* mean,
+                               void* stream) {
+  if (!planes || !origin || !mean) return set_error(ZR_EINVAL, "zr_full_prepare: null argument");
+  if (n <= 0) return ZR_OK;
+  if (C < 32 || C > 8192 || (C & 1)) return set_error(ZR_ESIZE, "zr_full_prepare: plane side %d", C);
+  k_full_prepare<<<n, 1024, 0, (cudaStream_t)stream>>>(planes, C, suppress_origin, origin, mean);
+  return launched("k_full_prepare");
+}
+
+extern "C" size_t zr_full_work_bytes(int n_planes, int C) {
+  const size_t filt_part = (size_t)n_planes * full_blocks(C) * 3 * sizeof(double);
+  const size_t mask_part = (size_t)n_planes * FP_MBLK * 5 * sizeof(double);
+  return (size_t)n_planes * C * C * sizeof(float) + (filt_part > mask_part ? filt_part : mask_part);
+}
+
+extern "C" int zr_full_filter(const float* planes, int n_planes, int C, const int* sel, int n_sel,
+                              const float* weights, const int* radius, const float* mean, float* filtered,
+                              double* stats, void* work, size_t work_bytes, void* stream) {
+  if (!planes || !sel || !weights || !radius || !mean || !stats || !work)
+    return set_error(ZR_EINVAL, "zr_full_filter: null argument");
+  if (n_sel <= 0) return ZR_OK;
+  if (n_sel > n_planes || C < 32 || C > 8192) return set_error(ZR_EINVAL, "zr_full_filter: bad sizes");
+  if (work_bytes < zr_full_work_bytes(n_planes, C))
+    return set_error(ZR_EWORK, "zr_full_filter: work buffer %zu < %zu", work_bytes, zr_full_work_bytes(n_planes, C));
+  cudaStream_t st = (cudaStream_t)stream;
+  float* tmp = (float*)work;
+  double* part = (double*)((char*)work + (size_t)n_planes * C * C * sizeof(float));
+  const dim3 grid((C + FP_TX - 1) / FP_TX, (C + FP_RY - 1) / FP_RY, n_sel);
+  k_full_vert<<<grid, FP_T, 0, st>>>(planes, C, sel, weights, radius, tmp);
+  ZR_TRY(launched("k_full_vert"));
+  k_full_horz<<<grid, FP_T, 0, st>>>(tmp, C, sel, weights, radius, mean, filtered, part);
+  ZR_TRY(launched("k_full_horz"));
+  k_full_reduce<<<n_sel, 32, 0, st>>>(part, full_blocks(C), sel, stats);
+  return launched("k_full_reduce");
+}
+
+extern "C" int zr_full_peaks(const float* planes, const float* filtered, int n_planes, int C, const int* sel,
+                             int n_sel, int max_shift, const int* rolls, const float* mean, const float* origin,
+                             const double* sigma, const int* nfev, int sub_pix_reg, zr_peak_result_t* results,
+                             void* work, size_t work_bytes, void* stream) {
+  if (!planes || !filtered || !sel || !rolls || !mean || !origin || !sigma || !nfev || !results || !work)
+    return set_error(ZR_EINVAL, "zr_full_peaks: null argument");
+  if (n_sel <= 0) return ZR_OK;
+  if (n_sel > n_planes || C < 32 || C > 8192 || max_shift <= 0) return set_error(ZR_EINVAL, "zr_full_peaks: bad sizes");
+  if (sub_pix_reg > 1 && (TWN % (16 * sub_pix_reg) != 0 || 16 * sub_pix_reg > 512))
+    return set_error(ZR_ESIZE, "zr_full_peaks: subPixReg %d must be a power of two <= 32", sub_pix_reg);
+  if (work_bytes < zr_full_work_bytes(n_planes, C))
+    return set_error(ZR_EWORK, "zr_full_peaks: work buffer %zu < %zu", work_bytes, zr_full_work_bytes(n_planes, C));
+  const float2* tw = twiddles();
+  if (!tw) return ZR_ECUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  double* part = (double*)((char*)work + (size_t)n_planes * C * C * sizeof(float));
+  k_full_masked<<<dim3(FP_MBLK, 1, n_sel), FP_T, 0, st>>>(filtered, C, sel, max_shift, rolls, mean, part);
+  ZR_TRY(launched("k_full_masked"));
+  const size_t smem = sub_pix_reg > 1 ? (size_t)17 * 16 * sub_pix_reg * sizeof(float2) : 16;
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_full_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_full_finish attr"));
+  k_full_finish<<<n_sel, PK_T, smem, st>>>(planes, filtered, C, sel, part, mean, origin, sigma, nfev, sub_pix_reg,
+                                           results, tw);
+  return launched("k_full_finish");
 }

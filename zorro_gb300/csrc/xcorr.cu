@@ -328,8 +328,8 @@ static int run_jobs(XcJobs J, int njobs, int C0, int C1, int mS, const float* te
 static int check_sizes(int C0, int C1, int mS) {
   if (!fft_len_ok(C0) || !fft_len_ok(C1) || C0 < 64 || C1 < 64 || C0 > 4096 || C1 > 4096)
     return set_error(ZR_ESIZE, "crop %dx%d must be powers of two in [64, 4096] or 3 x 2^k in [384, 3072]", C0, C1);
-  if (mS < 2 || 2 * mS > C0 || 2 * mS > C1 || mS > 112)
-    return set_error(ZR_ESIZE, "maxShift %d must satisfy 2 <= maxShift <= min(112, C/2)", mS);
+  if (mS < 2 || 2 * mS > C0 || 2 * mS > C1)
+    return set_error(ZR_ESIZE, "maxShift %d must satisfy 2 <= maxShift <= C/2", mS);
   return ZR_OK;
 }
 

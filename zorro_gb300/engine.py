@@ -32,6 +32,10 @@ from . import _lib
 from . import hostmath as hm
 from ._lib import Frames, HotpixParams, PeakParams, PeakResult, Shift, DoseParams
 
+# host view of zr_peak_result_t
+_PEAK_DTYPE = np.dtype([("sy", "f8"), ("sx", "f8"), ("sigma", "f8"), ("corr", "f4"), ("peaksig", "f4"),
+                        ("origin", "f4"), ("cy", "i4"), ("cx", "i4"), ("flags", "i4"), ("nfev", "i4")], align=True)
+
 _RAW_TYPES = {np.dtype(np.float32): _lib.ZR_F32, np.dtype(np.uint8): _lib.ZR_U8, np.dtype(np.uint16): _lib.ZR_U16,
               np.dtype(np.float16): _lib.ZR_F16}
 
@@ -272,13 +276,210 @@ class Engine:
                       ha.data_ptr() if ha is not None else None, hb.data_ptr() if hb is not None else None,
                       float(gdiv), N, H, W, 0)
 
+    def _cropped_peaks(self, reg, pairs, refine, N, C0, C1, mS, pp, spec, st):
+        """The +/-maxShift correlation windows of every pair (mnxc2,
+        zorro.py:1014-1097) and their peaks (locatePeak, one CTA a window).
+        Returns the peak records, one per pair."""
+        torch = self.torch
+        half, G, S, GM, G16, S16, GM16, hsc = spec
+        M = len(pairs)
+        w = 2 * mS
+        se = int(GM.shape[0])
+        terms = self.tensor("terms", (4 * N + 1, w, w), torch.float32)
+        xw = min(XCORR_WORK, max(self.lib.zr_xcorr_work_bytes(1, C1, mS), self.lib.zr_xcorr_work_bytes(M, C1, mS)))
+        xptr = self.ptr("xcwork", xw)
+        if half:
+            # products, inverse transforms and the combination stay float32
+            self.call("D_frame_terms", "zr_xcorr_terms_half", G16.data_ptr(), S16.data_ptr(), GM16.data_ptr(),
+                      hsc.data_ptr(), N, C0, C1, mS, terms.data_ptr(), xptr, xw, st)
+        else:
+            self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), N, C0, C1, mS,
+                      terms.data_ptr(), xptr, xw, st)
+        cwin = self.tensor("cwin", (max(M, 1), w, w), torch.float32)
+        if refine:
+            TG = self.tensor("refineT", (N, se, 2), torch.float32)
+            rterms = self.tensor("refine_terms", (4 * N + 1, w, w), torch.float32)
+            self.call("E_pairs", "zr_refine_spectra", G.data_ptr(), N, C0, C1, TG.data_ptr(), st)
+            self.call("E_pairs", "zr_refine_terms", terms.data_ptr(), N, mS, rterms.data_ptr(), st)
+            self.call("E_pairs", "zr_xcorr_refine", G.data_ptr(), TG.data_ptr(), rterms.data_ptr(), N, C0, C1, mS,
+                      cwin.data_ptr(), xptr, xw, st)
+        elif half:
+            pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
+            self.call("E_pairs", "zr_xcorr_pairs_half", G16.data_ptr(), hsc.data_ptr(), terms.data_ptr(),
+                      pairs_dev.data_ptr(), M, N, C0, C1, mS, cwin.data_ptr(), xptr, xw, st)
+        else:
+            pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
+            self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pairs_dev.data_ptr(), M, N, C0, C1,
+                      mS, cwin.data_ptr(), xptr, xw, st)
+        pres = self.tensor("peaks", (max(M, 1), C.sizeof(PeakResult)), torch.uint8)
+        self.call("F_peaks", "zr_locate_peaks", cwin.data_ptr(), M, mS, C.byref(pp), pres.data_ptr(), st)
+        host = pres[:M].cpu().numpy()
+        return np.frombuffer(host.tobytes(), dtype=_PEAK_DTYPE).copy()
+
+    def _preshift(self, reg, pairs, refine, N, C0, C1, pp, spec, st):
+        """preShift (zorro.py:1089-1092, 1148-1168): whole C x C correlation
+        planes, searched within the maxShift disc rolled to the rounded shift
+        of the previous pair of the row (shiftsTriMat[I, J-1], in cropped
+        pixels as measured so far; 'refine': shiftsTriMat[I-1, I-1]).  A pair
+        depends only on its left neighbour in its row, so the pairs go
+        diagonal by diagonal (all J - I = d together; 'refine' one frame at a
+        time).  The planes of a diagonal are searched together: the host
+        steps the bounded Brent search over sigma of every plane in lock
+        step, each step one batched filter launch.  Returns the peak records
+        and which pairs were measured ('auto' stops a row as the reference
+        does)."""
+        import math
+        torch = self.torch
+        if C0 != C1:
+            raise ValueError("preShift needs a square Fourier crop: the reference builds its search mask with the "
+                             "crop's axes swapped (zorro.py:843-844), which does not fit a %dx%d plane" % (C0, C1))
+        half, G, S, GM, G16, S16, GM16, hsc = spec
+        M = len(pairs)
+        mS = int(reg.maxShift)
+        mSf, wf = C0 // 2, C0
+        se = int(GM.shape[0])
+        terms = self.tensor("terms", (4 * N + 1, wf, wf), torch.float32)
+        xw = max(self.lib.zr_xcorr_work_bytes(1, C1, mSf),
+                 min(XCORR_WORK, self.lib.zr_xcorr_work_bytes(max(M, 1), C1, mSf)))
+        xptr = self.ptr("xcwork", xw)
+        if half:
+            self.call("D_frame_terms", "zr_xcorr_terms_half", G16.data_ptr(), S16.data_ptr(), GM16.data_ptr(),
+                      hsc.data_ptr(), N, C0, C1, mSf, terms.data_ptr(), xptr, xw, st)
+        else:
+            self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), N, C0, C1, mSf,
+                      terms.data_ptr(), xptr, xw, st)
+        if refine:
+            groups = [[k] for k in range(M)]
+            npl = max(M, 1)
+        else:
+            d = pairs[:, 1] - pairs[:, 0]
+            groups = [[int(k) for k in np.nonzero(d == v)[0]] for v in np.unique(d)]
+            npl = max([len(g) for g in groups] + [1])
+        planes = self.tensor("full_planes", (npl, wf, wf), torch.float32)
+        filt = self.tensor("full_filt", (npl, wf, wf), torch.float32)
+        if refine:
+            TG = self.tensor("refineT", (N, se, 2), torch.float32)
+            rterms = self.tensor("refine_terms", (4 * N + 1, wf, wf), torch.float32)
+            self.call("E_pairs", "zr_refine_spectra", G.data_ptr(), N, C0, C1, TG.data_ptr(), st)
+            self.call("E_pairs", "zr_refine_terms", terms.data_ptr(), N, mSf, rterms.data_ptr(), st)
+            self.call("E_pairs", "zr_xcorr_refine", G.data_ptr(), TG.data_ptr(), rterms.data_ptr(), N, C0, C1, mSf,
+                      planes.data_ptr(), xptr, xw, st)
+        fw = self.lib.zr_full_work_bytes(npl, wf)
+        fptr = self.ptr("full_work", fw)
+        mean = self.tensor("full_mean", (npl,), torch.float32)
+        origin = self.tensor("full_origin", (npl,), torch.float32)
+        stats = self.tensor("full_stats", (npl, 3), torch.float64)
+        taps = self.tensor("full_taps", (npl, 2, 129), torch.float32)
+        rad = self.tensor("full_rad", (npl, 2), torch.int32)
+        sel = self.tensor("full_sel", (npl,), torch.int32)
+        rolls = self.tensor("full_rolls", (npl, 2), torch.int32)
+        sig = self.tensor("full_sigma", (npl,), torch.float64)
+        nfe = self.tensor("full_nfev", (npl,), torch.int32)
+        res = self.tensor("full_res", (npl, C.sizeof(PeakResult)), torch.uint8)
+        taps_h = np.zeros((npl, 2, 129), np.float32)
+        rad_h = np.zeros((npl, 2), np.int32)
+        pr = np.zeros(M, dtype=_PEAK_DTYPE)
+        keep = np.zeros(M, dtype=bool)
+        sh_un = np.zeros((N, N, 2))
+        row_done = set()
+        auto = reg.triMode == "auto"
+        npx = float(wf) * float(wf)
+
+        def filter_planes(idx, sy, sx, keep_filtered):
+            for p, a, b in zip(idx, sy, sx):
+                for axis, sg in ((0, a), (1, b)):
+                    t, r = hm.gaussian_taps(sg)
+                    taps_h[p, axis, :] = 0.0
+                    taps_h[p, axis, :t.size] = t
+                    rad_h[p, axis] = r
+            taps.copy_(torch.from_numpy(taps_h))
+            rad.copy_(torch.from_numpy(rad_h))
+            sel[:len(idx)].copy_(torch.from_numpy(np.asarray(idx, dtype=np.int32)))
+            self.call("F_peaks", "zr_full_filter", planes.data_ptr(), npl, wf, sel.data_ptr(), len(idx),
+                      taps.data_ptr(), rad.data_ptr(), mean.data_ptr(),
+                      filt.data_ptr() if keep_filtered else None, stats.data_ptr(), fptr, fw, st)
+
+        for g in groups:
+            ks = [k for k in g if not (auto and int(pairs[k][0]) in row_done)]
+            if not ks:
+                continue
+            n = len(ks)
+            if refine:
+                idx = ks
+                for k in ks:
+                    self.call("F_peaks", "zr_full_prepare", planes[k].data_ptr(), 1, wf, pp.suppress_origin,
+                              origin[k:].data_ptr(), mean[k:].data_ptr(), st)
+            else:
+                idx = list(range(n))
+                pd = torch.from_numpy(np.ascontiguousarray(pairs[ks], dtype=np.int32).reshape(-1)).to(self.dev)
+                if half:
+                    self.call("E_pairs", "zr_xcorr_pairs_half", G16.data_ptr(), hsc.data_ptr(), terms.data_ptr(),
+                              pd.data_ptr(), n, N, C0, C1, mSf, planes.data_ptr(), xptr, xw, st)
+                else:
+                    self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pd.data_ptr(), n, N, C0,
+                              C1, mSf, planes.data_ptr(), xptr, xw, st)
+                self.call("F_peaks", "zr_full_prepare", planes.data_ptr(), n, wf, pp.suppress_origin,
+                          origin.data_ptr(), mean.data_ptr(), st)
+            nf = np.zeros(n, dtype=np.int32)
+            sigma = np.full(n, np.nan)
+            if pp.bmode == 1:
+                gens = [hm.brent_bounded(pp.opti_lo, pp.opti_hi, pp.opti_xatol, pp.opti_maxiter) for _ in ks]
+                xs = [next(gn) for gn in gens]
+                act = list(range(n))
+                while act:
+                    filter_planes([idx[i] for i in act], [xs[i] for i in act], [xs[i] for i in act], False)
+                    sth = stats.cpu().numpy()
+                    mh = mean.cpu().numpy().astype(np.float64)
+                    nxt = []
+                    for i in act:
+                        s1, s2, mx = sth[idx[i]]
+                        m1 = s1 / npx
+                        var = s2 / npx - m1 * m1
+                        with np.errstate(all="ignore"):
+                            f = float(np.float64(math.sqrt(var if var > 0.0 else 0.0)) / np.float64(mx - (mh[idx[i]] + m1)))
+                        try:
+                            xs[i] = gens[i].send(f)
+                            nxt.append(i)
+                        except StopIteration as stop:
+                            sigma[i], nf[i] = stop.value
+                    act = nxt
+                sy = sx = list(sigma)
+            elif pp.bmode == 2:
+                sy, sx = [pp.conv_sigma_y] * n, [pp.conv_sigma_x] * n
+            else:
+                sy = sx = [0.0] * n
+            filter_planes(idx, sy, sx, True)
+            rolls_h = np.zeros((npl, 2), np.int32)
+            sig_h = np.full(npl, np.nan)
+            nf_h = np.zeros(npl, np.int32)
+            for i, k in enumerate(ks):
+                I, J = int(pairs[k][0]), int(pairs[k][1])
+                prev = sh_un[I - 1, I - 1] if refine else sh_un[I, J - 1]
+                rolls_h[idx[i]] = np.round(prev).astype(np.int32)
+                sig_h[idx[i]] = sigma[i]
+                nf_h[idx[i]] = nf[i]
+            rolls.copy_(torch.from_numpy(rolls_h))
+            sig.copy_(torch.from_numpy(sig_h))
+            nfe.copy_(torch.from_numpy(nf_h))
+            self.call("F_peaks", "zr_full_peaks", planes.data_ptr(), filt.data_ptr(), npl, wf, sel.data_ptr(), n, mS,
+                      rolls.data_ptr(), mean.data_ptr(), origin.data_ptr(), sig.data_ptr(), nfe.data_ptr(),
+                      pp.sub_pix_reg, res.data_ptr(), fptr, fw, st)
+            recs = np.frombuffer(res.cpu().numpy().tobytes(), dtype=_PEAK_DTYPE)
+            for i, k in enumerate(ks):
+                r = recs[idx[i]]
+                pr[k] = r
+                keep[k] = True
+                I, J = int(pairs[k][0]), int(pairs[k][1])
+                sh_un[I, J] = (r["sy"], r["sx"])
+                if auto and (r["peaksig"] <= reg.peaksigThres or J - I >= reg.autoMax):
+                    row_done.add(I)
+        return pr, keep
+
     def _align(self, reg):
         torch = self.torch
         st = self.stream
         bench = {}
         bench["align0"] = time.time()
-        if reg.preShift:
-            raise ValueError("preShift is not supported by the GPU path")
         if reg.shiftMethod == "fourier":
             # the reference stops in xcorrnm2_tri while storing the full spectra
             # that shift method needs (self.__sC2 is undefined, zorro.py:891-895)
@@ -439,32 +640,6 @@ class Engine:
             tri = hm.tri_indices(N, reg.triMode, reg.diagWidth, reg.diagStart)
             pairs = hm.pair_list(tri)
         M = len(pairs)
-        terms = self.tensor("terms", (4 * N + 1, w, w), torch.float32)
-        xw = min(XCORR_WORK, max(self.lib.zr_xcorr_work_bytes(1, C1, mS), self.lib.zr_xcorr_work_bytes(M, C1, mS)))
-        xptr = self.ptr("xcwork", xw)
-        if half:
-            # products, inverse transforms and the combination stay float32
-            self.call("D_frame_terms", "zr_xcorr_terms_half", G16.data_ptr(), S16.data_ptr(), GM16.data_ptr(),
-                      hsc.data_ptr(), N, C0, C1, mS, terms.data_ptr(), xptr, xw, st)
-        else:
-            self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), N, C0, C1, mS,
-                      terms.data_ptr(), xptr, xw, st)
-        cwin = self.tensor("cwin", (max(M, 1), w, w), torch.float32)
-        if refine:
-            TG = self.tensor("refineT", (N, se, 2), torch.float32)
-            rterms = self.tensor("refine_terms", (4 * N + 1, w, w), torch.float32)
-            self.call("E_pairs", "zr_refine_spectra", G.data_ptr(), N, C0, C1, TG.data_ptr(), st)
-            self.call("E_pairs", "zr_refine_terms", terms.data_ptr(), N, mS, rterms.data_ptr(), st)
-            self.call("E_pairs", "zr_xcorr_refine", G.data_ptr(), TG.data_ptr(), rterms.data_ptr(), N, C0, C1, mS,
-                      cwin.data_ptr(), xptr, xw, st)
-        elif half:
-            pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
-            self.call("E_pairs", "zr_xcorr_pairs_half", G16.data_ptr(), hsc.data_ptr(), terms.data_ptr(),
-                      pairs_dev.data_ptr(), M, N, C0, C1, mS, cwin.data_ptr(), xptr, xw, st)
-        else:
-            pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
-            self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pairs_dev.data_ptr(), M, N, C0, C1,
-                      mS, cwin.data_ptr(), xptr, xw, st)
         pp = PeakParams()
         pp.sub_pix_reg = int(reg.subPixReg or 1)
         bm = str(reg.Bmode)
@@ -481,27 +656,26 @@ class Engine:
         pp.suppress_origin = int(bool(reg.suppressOrigin))
         pp.use_mask = 1
         pp.opti_lo, pp.opti_hi, pp.opti_xatol, pp.opti_maxiter = 0.0, 7.0, 0.01, 15
-        pres = self.tensor("peaks", (max(M, 1), C.sizeof(PeakResult)), torch.uint8)
-        self.call("F_peaks", "zr_locate_peaks", cwin.data_ptr(), M, mS, C.byref(pp), pres.data_ptr(), st)
-        host = pres[:M].cpu().numpy()
-        pr = np.frombuffer(host.tobytes(), dtype=np.dtype([("sy", "f8"), ("sx", "f8"), ("sigma", "f8"), ("corr", "f4"),
-                                                           ("peaksig", "f4"), ("origin", "f4"), ("cy", "i4"),
-                                                           ("cx", "i4"), ("flags", "i4"), ("nfev", "i4")],
-                                                          align=True))
+        spec = (half, G, S, GM, G16 if half else None, S16 if half else None, GM16 if half else None,
+                hsc if half else None)
+        if reg.preShift and mS:
+            pr, keep = self._preshift(reg, pairs, refine, N, C0, C1, pp, spec, st)
+        else:
+            pr = self._cropped_peaks(reg, pairs, refine, N, C0, C1, mS, pp, spec, st)
+            keep = np.ones(M, dtype=bool)
+            if reg.triMode == "auto":
+                row_done = {}
+                for k, (I, J) in enumerate(pairs):
+                    if row_done.get(I):
+                        keep[k] = False
+                        continue
+                    if pr["peaksig"][k] <= reg.peaksigThres or J - I >= reg.autoMax:
+                        row_done[I] = True
         bench["xcorr2"] = time.time()
         shifts = np.zeros([N, N, 2])
         corr = np.zeros([N, N])
         psig = np.zeros([N, N])
         orig = np.zeros([N, N])
-        keep = np.ones(M, dtype=bool)
-        if reg.triMode == "auto":
-            row_done = {}
-            for k, (I, J) in enumerate(pairs):
-                if row_done.get(I):
-                    keep[k] = False
-                    continue
-                if pr["peaksig"][k] <= reg.peaksigThres or J - I >= reg.autoMax:
-                    row_done[I] = True
         Ii, Jj = pairs[keep, 0], pairs[keep, 1]
         shifts[Ii, Jj, 0] = pr["sy"][keep]
         shifts[Ii, Jj, 1] = pr["sx"][keep]

@@ -10,6 +10,7 @@ follows.  The GPU does every pass over pixels.
 from __future__ import annotations
 
 import concurrent.futures
+import math
 
 import numpy as np
 import scipy.optimize
@@ -210,6 +211,99 @@ def solve_shifts(shiftsTriMat_in, corrTriMat_in, peaksigTriMat_in, *, shapeImage
                "errorX": errorX, "errorY": errorY, "errorUnraveled": errorUnraveled, "mean_errorNorm": mean_e,
                "std_errorNorm": std_e, "M": M, "Maccepted": M})
     return ed
+
+
+def _sgn1(v):
+    return -1.0 if v < 0.0 else 1.0
+
+
+def brent_bounded(lo, hi, xatol, maxfun):
+    """Bounded Brent minimisation (golden section and parabolic steps, the
+    FMIN method of Forsythe, Malcolm and Moler behind scipy's
+    minimize_scalar(method='bounded'), which locatePeak calls at
+    zorro.py:1117) as a generator: it yields each abscissa, receives its
+    function value through send(), and returns the best abscissa and the
+    number of function values (StopIteration.value).  The steps are those
+    of the peak kernel's device search, so that many planes can be searched
+    in lock step with one batched evaluation per step."""
+    sqrt_eps = math.sqrt(2.2e-16)
+    golden = 0.5 * (3.0 - math.sqrt(5.0))
+    a, b = lo, hi
+    fulc = a + golden * (b - a)
+    nfc = xf = fulc
+    rat = e = 0.0
+    x = xf
+    fx = yield x
+    num = 1
+    ffulc = fnfc = fx
+    xm = 0.5 * (a + b)
+    tol1 = sqrt_eps * abs(xf) + xatol / 3.0
+    tol2 = 2.0 * tol1
+    while abs(xf - xm) > (tol2 - 0.5 * (b - a)):
+        gstep = True
+        if abs(e) > tol1:
+            gstep = False
+            r = (xf - nfc) * (fx - ffulc)
+            q = (xf - fulc) * (fx - fnfc)
+            p = (xf - fulc) * q - (xf - nfc) * r
+            q = 2.0 * (q - r)
+            if q > 0.0:
+                p = -p
+            q = abs(q)
+            r = e
+            e = rat
+            if abs(p) < abs(0.5 * q * r) and p > q * (a - xf) and p < q * (b - xf):
+                rat = (p + 0.0) / q
+                x = xf + rat
+                if (x - a) < tol2 or (b - x) < tol2:
+                    rat = tol1 * _sgn1(xm - xf)
+            else:
+                gstep = True
+        if gstep:
+            e = (a - xf) if xf >= xm else (b - xf)
+            rat = golden * e
+        x = xf + _sgn1(rat) * max(abs(rat), tol1)
+        fu = yield x
+        num += 1
+        if fu <= fx:
+            if x >= xf:
+                a = xf
+            else:
+                b = xf
+            fulc, ffulc = nfc, fnfc
+            nfc, fnfc = xf, fx
+            xf, fx = x, fu
+        else:
+            if x < xf:
+                a = x
+            else:
+                b = x
+            if fu <= fnfc or nfc == xf:
+                fulc, ffulc = nfc, fnfc
+                nfc, fnfc = x, fu
+            elif fu <= ffulc or fulc == xf or fulc == nfc:
+                fulc, ffulc = x, fu
+        xm = 0.5 * (a + b)
+        tol1 = sqrt_eps * abs(xf) + xatol / 3.0
+        tol2 = 2.0 * tol1
+        if num >= maxfun:
+            break
+    return xf, num
+
+
+def gaussian_taps(sigma, max_radius=64):
+    """Taps of scipy.ndimage.gaussian_filter1d with truncate 4: radius
+    int(4 sigma + 0.5), exp(-k^2 / (2 sigma^2)) normalised in double, as
+    float32; one tap of 1 when sigma is 0 (the axis is not filtered)."""
+    if not sigma > 1e-15:
+        return np.ones(1, dtype=np.float32), 0
+    r = min(int(4.0 * sigma + 0.5), max_radius)
+    c = -0.5 / (sigma * sigma)
+    g = [math.exp(c * k * k) for k in range(-r, r + 1)]
+    s = 0.0
+    for v in g:
+        s += v
+    return np.array([v / s for v in g], dtype=np.float32), r
 
 
 def lanczos_kernel_1d(frac):
