@@ -7,8 +7,9 @@ Workload (the K2 configuration): 40 frames of 3838 x 3710 uint8 counts
 (Poisson mean 0.8 e/px/frame) with a U(0.9, 1.1) float32 gain map and 0.01 %
 hot pixels at 50x the mean, random-walk drift 1.2 px/frame; padded to 4096,
 Fourier-cropped to 2048 for the all-pairs triangle (780 pairs, maxShift 100),
-hot-pixel filter, Lanczos shift and sum, lazy even/odd FRC and the dose
-filter at 1.2 e/A^2/frame, 1.05 A/px.  Inputs are seeded synthetic movies.
+hot-pixel filter, Lanczos shift and sum, the independent even/odd FRC (the
+even and the odd frames registered again, their sums aligned, tiled FRC)
+and the dose filter at 1.2 e/A^2/frame, 1.05 A/px.  Inputs are seeded synthetic movies.
 
 One step registers one movie.  ``value`` is movies/s with the raw frames
 already resident in HBM; ``e2e`` is the same through the public API from
@@ -47,14 +48,14 @@ WORKLOADS = {
                           gain_map=True, hot_fraction=1e-4, hot_factor=50.0),
                attrs=dict(triMode="tri", shapePadded=[4096, 4096], fouCrop=[2048, 2048], maxShift=100,
                           pixelsize=0.105, voltage=300.0, filterMode="hot,dose", doseFiltParam=K2_DOSE,
-                          subPixReg=16, shiftMethod="lanczos", Bmode="opti", doLazyFRC=True)),
+                          subPixReg=16, shiftMethod="lanczos", Bmode="opti", doEvenOddFRC=True)),
     # the K2 movie cut to 10 frames (142 MB of raw frames, still larger than L2): the case the
     # per-kernel ncu captures run on
     "k2x10": dict(movie=dict(n_frames=10, shape=(3838, 3710), seed=2024, mean_dose=0.8, drift_sigma=1.2,
                              dtype="uint8", gain_map=True, hot_fraction=1e-4, hot_factor=50.0),
                   attrs=dict(triMode="tri", shapePadded=[4096, 4096], fouCrop=[2048, 2048], maxShift=100,
                              pixelsize=0.105, voltage=300.0, filterMode="hot,dose", doseFiltParam=K2_DOSE,
-                             subPixReg=16, shiftMethod="lanczos", Bmode="opti", doLazyFRC=True)),
+                             subPixReg=16, shiftMethod="lanczos", Bmode="opti", doEvenOddFRC=True)),
     "small": dict(movie=dict(n_frames=20, shape=(1024, 1024), seed=1, mean_dose=1.0, drift_sigma=0.8),
                   attrs=dict(triMode="tri", shapePadded=[1024, 1024], fouCrop=[1024, 1024], maxShift=40,
                              pixelsize=0.1, voltage=300.0, filterMode="dose",
@@ -64,27 +65,47 @@ METRIC = "4k x 4k x 40 movies/sec (K2 3838x3710x40 registration)"
 UNIT = "movies/s"
 
 
-def algorithmic_bytes(N, H, W, C, w, M, b_in):
+def algorithmic_bytes(N, H, W, C, w, M, b_in, evenodd=False, hot=True):
     """Unique logical bytes per movie and stage: every input element read once,
-    every output written once (FFT intermediates excluded)."""
+    every output written once (FFT intermediates excluded).  With ``evenodd``
+    the two half-set registrations of the independent FRC (n = N/2 aligned
+    float32 frames each, hot filter, spectra, terms, the half triangle,
+    shift-sum) and the 'first' alignment of the two sums are added to the
+    stages they run in."""
     HW = H * W
     spec = C * (C // 2 + 1) * 8
-    return {"A_gain_sum": N * HW * b_in + 8 * HW, "B_hot_maps": 12 * HW,
-            "C_spectra": N * HW * b_in + 12 * HW + 2 * N * spec, "D_frame_terms": 2 * N * spec + 16 * N * w * w,
-            "E_pairs": N * spec + 4 * M * w * w, "F_peaks": 4 * M * w * w, "G_shift_sum": N * HW * b_in + 24 * HW,
-            "H_frc": 8 * HW, "I_dose": N * HW * b_in + 16 * HW}
+
+    def one(n, m, b, hotpix):
+        return {"A_gain_sum": (n * HW * b + 8 * HW) if hotpix else 0, "B_hot_maps": 12 * HW if hotpix else 0,
+                "C_spectra": n * HW * b + 12 * HW + 2 * n * spec, "D_frame_terms": 2 * n * spec + 16 * n * w * w,
+                "E_pairs": n * spec + 4 * m * w * w, "F_peaks": 4 * m * w * w, "G_shift_sum": n * HW * b + 24 * HW}
+    ab = one(N, M, b_in, True)
+    ab["H_frc"] = 8 * HW
+    ab["I_dose"] = N * HW * b_in + 16 * HW
+    if evenodd:
+        n = N // 2
+        for part in (one(n, n * (n - 1) // 2, 4, hot), one(n, n * (n - 1) // 2, 4, hot), one(2, 1, 4, False)):
+            for k, v in part.items():
+                ab[k] += v
+    return ab
 
 
-def fft_flops(N, P, C, w, M):
+def fft_flops(N, P, C, w, M, evenodd=False):
     """Nominal FFT FLOPs per movie and stage, 5 n log2(n) per complex
     transform of n points (a real transform counts half).  A pruned inverse
     (columns at C, then only the w kept rows) costs (C/2 + 1 + w/2) column/row
-    transforms of length C."""
+    transforms of length C.  ``evenodd`` adds the half-set registrations."""
     import math
     full_real = 2.5 * P * P * math.log2(P * P)
     pruned = (C // 2 + 1 + w // 2) * 5.0 * C * math.log2(C)
-    return {"C_spectra": 2 * N * full_real, "D_frame_terms": (4 * N + 1) * pruned, "E_pairs": M * pruned,
-            "I_dose": (N + 1) * full_real}
+    fl = {"C_spectra": 2 * N * full_real, "D_frame_terms": (4 * N + 1) * pruned, "E_pairs": M * pruned,
+          "I_dose": (N + 1) * full_real}
+    if evenodd:
+        n = N // 2
+        fl["C_spectra"] += 2 * (2 * n * full_real) + 2 * 2 * full_real
+        fl["D_frame_terms"] += 2 * (4 * n + 1) * pruned + 9 * pruned
+        fl["E_pairs"] += 2 * (n * (n - 1) // 2) * pruned + pruned
+    return fl
 
 
 def read_traffic():
@@ -225,10 +246,20 @@ def cpu_sample(mv, attrs, workers, pairs=2, frames=1, full_steps=False):
         zo.dose_filter(imgs[:frames], P, attrs["pixelsize"], 300.0, attrs["doseFiltParam"],
                        np.zeros((H, W), np.float32), dt=dt)
     t["dose_per_frame"] = (time.perf_counter() - t0) / frames
-    movie_s = t["hot"] + N * (t["spectra_per_frame"] + t["shift_per_frame"] + t["dose_per_frame"]) + M * t["pair"]
+    per_frame = t["spectra_per_frame"] + t["shift_per_frame"] + t["dose_per_frame"]
+    movie_s = t["hot"] + N * per_frame + M * t["pair"]
+    extra = ""
+    if attrs.get("doEvenOddFRC"):
+        # evenOddFouRingCorr (zorro.py:2099-2224): the even and the odd frames
+        # registered again with the saved settings (hot filter, spectra, the
+        # half triangle, shifts, dose), then the two sums in 'first' mode
+        n = N // 2
+        Mh = n * (n - 1) // 2
+        movie_s += 2 * (t["hot"] * n / N + n * per_frame + Mh * t["pair"]) + 2 * t["spectra_per_frame"] + t["pair"]
+        extra = " + two half-set registrations of %d frames / %d pairs and the 'first' pair of the sums" % (n, Mh)
     return movie_s, t, "hot-pixel filter of the full stack %s, spectra of %d frames, %d of %d pairs, shift and dose " \
-        "of %d frame(s); scaled to %d frames / %d pairs" % ("(timed)" if full_steps else "(not in sample)",
-                                                             max(frames, 2), pairs, M, frames, N, M)
+        "of %d frame(s); scaled to %d frames / %d pairs%s" % ("(timed)" if full_steps else "(not in sample)",
+                                                               max(frames, 2), pairs, M, frames, N, M, extra)
 
 
 def run_reference(args, wl, rank, world):
@@ -484,14 +515,15 @@ def main():
     w = 2 * wl["attrs"]["maxShift"]
     C = int(wl["attrs"]["fouCrop"][0])
     M = N * (N - 1) // 2 if wl["attrs"]["triMode"] == "tri" else None
-    ab = algorithmic_bytes(N, H, W, C, w, M, b_in)
+    evenodd = bool(wl["attrs"].get("doEvenOddFRC"))
+    ab = algorithmic_bytes(N, H, W, C, w, M, b_in, evenodd=evenodd, hot="hot" in wl["attrs"].get("filterMode", ""))
     per_step = {k: v / args.steps for k, v in stage_ms.items()}
     dom = max(per_step, key=per_step.get)
     peak, peak_kind = measured_peaks()
     achieved = ab[dom] / (per_step[dom] / 1000.0) / 1e9
     traffic = read_traffic().get(dom) if args.workload == "k2" else None
     P = int(wl["attrs"]["shapePadded"][0])
-    fl = fft_flops(N, P, C, w, M if M is not None else N - 1)
+    fl = fft_flops(N, P, C, w, M if M is not None else N - 1, evenodd=evenodd)
     # FP32 CUDA-core peak: 152 SMs x 128 lanes x 2 FLOP x SM clock
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind,
@@ -520,7 +552,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded K2-size movies)",
                 "config": {"workload": args.workload + ": 40x3838x3710 u8 + gain + 0.01% hot px, P=4096, C=2048, "
-                           "tri 780 pairs, maxShift 100, hot+dose filters, lazy FRC",
+                           "tri 780 pairs, maxShift 100, hot+dose filters, even/odd FRC (two "
+                           "half-set registrations of 20 frames)",
                            "l2": "inputs (570 MB raw frames per movie) larger than L2; no flush",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": round(world / t_e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,

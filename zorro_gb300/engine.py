@@ -21,6 +21,7 @@ Two exact reformulations of the reference's arithmetic are used:
 """
 from __future__ import annotations
 
+import concurrent.futures
 import contextlib
 import ctypes as C
 import threading
@@ -209,7 +210,7 @@ class Engine:
         for k, v in res.items():
             setattr(reg, k, v)
 
-    def _even_odd_frc(self, reg, aligned, hotinfo, filt):
+    def _even_odd_frc(self, reg, aligned, hotinfo, filt, ready=None):
         """Independent half-set FRC (evenOddFouRingCorr, zorro.py:2099-2224,
         xcorr='tri').  The even and odd frames of the aligned stack are
         registered again with the parent's settings (its hot-pixel filter
@@ -225,12 +226,14 @@ class Engine:
         N, H, W = (int(v) for v in aligned.shape)
         if N < 2:
             raise ValueError("doEvenOddFRC needs at least two frames")
-        # the half-set registrations read the aligned stack on their own stream
-        torch.cuda.current_stream(self.dev).synchronize()
+        # the half-set registrations read the aligned stack on their own streams,
+        # after ``ready`` (recorded once the stack was written)
+        if ready is None:
+            ready = torch.cuda.Event()
+            ready.record()
         parent = self._tls.slot["key"]
-        sub_slot = ("halfset", parent)
 
-        def register(images, **kw):
+        def register(images, sub_slot, **kw):
             r = ImageRegistrator()
             copy_config(reg, r)
             r.images = images
@@ -247,12 +250,19 @@ class Engine:
             r.bench = {}
             for k, v in kw.items():
                 setattr(r, k, v)
+            self._slot(sub_slot)["stream"].wait_event(ready)
             self.align(r, slot=sub_slot)
             return r
 
-        ev = register(aligned[0::2])
-        od = register(aligned[1::2])
-        eo = register(torch.stack([ev.imageSum, od.imageSum]), triMode="first", keepAlignedImages=True)
+        # the two halves are independent: the odd one on a second slot (its own
+        # stream and buffers) in a helper thread, so that one half's host steps
+        # (hot-pixel fit, drift solve) overlap the other's kernels
+        with concurrent.futures.ThreadPoolExecutor(1) as ex:
+            fut = ex.submit(register, aligned[1::2], ("halfset_odd", parent))
+            ev = register(aligned[0::2], ("halfset_even", parent))
+            od = fut.result()
+        eo = register(torch.stack([ev.imageSum, od.imageSum]), ("halfset_even", parent), triMode="first",
+                      keepAlignedImages=True)
         te, to = np.asarray(ev.translations), np.asarray(od.translations)
         box = 512
         offs, tiles = hm.frc_tiles((H, W), np.hstack([te, to]))
@@ -743,28 +753,11 @@ class Engine:
                   osum.data_ptr(), aligned.data_ptr() if aligned is not None else None, st)
         bench["shifts1"] = time.time()
 
-        # ---- lazy FRC (zorro.py:2226-2310)
-        frc = frc2d = None
-        if reg.doEvenOddFRC:
-            frc, frc2d, out["transEven"], out["transOdd"] = self._even_odd_frc(reg, aligned, hotinfo, filt)
-        elif reg.doLazyFRC:
-            offs, tiles = hm.frc_tiles((H, W), translations)
-            box = 512
-            if len(offs) and (offs.min() < 0 or (offs[:, 0] + box).max() > H or (offs[:, 1] + box).max() > W):
-                raise ValueError("tiledFRC: tiles %s leave the %dx%d image (negative crop limits)" % (tiles, H, W))
-            if len(offs) == 0:
-                frc = np.full(box // 2, np.nan)
-                frc2d = np.full((box, box), np.nan, dtype=np.float32)
-            else:
-                offs_dev = torch.from_numpy(offs.reshape(-1)).to(self.dev, non_blocking=True)
-                nr = box // 2
-                fwb = self.lib.zr_frc_work_bytes(len(offs), box)
-                f2 = self.tensor("frc2d", (box, box), torch.float32)
-                fr = self.tensor("frc", (nr,), torch.float64)
-                self.call("H_frc", "zr_tiled_frc", esum.data_ptr(), osum.data_ptr(), H, W, box, offs_dev.data_ptr(), len(offs),
-                          f2.data_ptr(), fr.data_ptr(), nr, self.ptr("frcwork", fwb), fwb, st)
-                frc2d, frc = f2, fr
-        bench["frc1"] = time.time()
+        # the aligned stack is complete here: the half-set registrations of the
+        # even/odd FRC wait on this event, not on the stream, so that the dose
+        # filter below runs on the GPU while they do their host steps
+        aligned_ready = torch.cuda.Event()
+        aligned_ready.record()
 
         # ---- dose filter (zorro.py:2349-2494)
         filt_sum = None
@@ -784,6 +777,31 @@ class Engine:
                 self.call("I_dose", "zr_dose_filter", aligned.data_ptr(), N, H, W, C.byref(dp), tq.data_ptr(), de.data_ptr(),
                           P0, P1, filt_sum.data_ptr(), self.ptr("dosework", dwb), dwb, st)
         bench["dose1"] = time.time()
+
+        # ---- lazy FRC (zorro.py:2226-2310)
+        frc = frc2d = None
+        if reg.doEvenOddFRC:
+            frc, frc2d, out["transEven"], out["transOdd"] = self._even_odd_frc(reg, aligned, hotinfo, filt,
+                                                                               aligned_ready)
+        elif reg.doLazyFRC:
+            offs, tiles = hm.frc_tiles((H, W), translations)
+            box = 512
+            if len(offs) and (offs.min() < 0 or (offs[:, 0] + box).max() > H or (offs[:, 1] + box).max() > W):
+                raise ValueError("tiledFRC: tiles %s leave the %dx%d image (negative crop limits)" % (tiles, H, W))
+            if len(offs) == 0:
+                frc = np.full(box // 2, np.nan)
+                frc2d = np.full((box, box), np.nan, dtype=np.float32)
+            else:
+                offs_dev = torch.from_numpy(offs.reshape(-1)).to(self.dev, non_blocking=True)
+                nr = box // 2
+                fwb = self.lib.zr_frc_work_bytes(len(offs), box)
+                f2 = self.tensor("frc2d", (box, box), torch.float32)
+                fr = self.tensor("frc", (nr,), torch.float64)
+                self.call("H_frc", "zr_tiled_frc", esum.data_ptr(), osum.data_ptr(), H, W, box, offs_dev.data_ptr(), len(offs),
+                          f2.data_ptr(), fr.data_ptr(), nr, self.ptr("frcwork", fwb), fwb, st)
+                frc2d, frc = f2, fr
+        bench["frc1"] = time.time()
+
 
         # ---- results back to the host (or left on the device)
         out["translations"] = translations

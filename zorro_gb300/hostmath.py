@@ -388,50 +388,46 @@ def hotpix_bins(sumMean, maxSigma):
     return sumMean, poissonStd, edges
 
 
-def _memo_last(f):
-    """f remembering its value at the last point it was called with:
-    L-BFGS-B asks for f and then for the gradient at the same point."""
-    last = [None, None]
+def _forward_points(x0, lb, ub, step, eps2):
+    """The points of scipy's 2-point forward difference with absolute step
+    ``step`` (approx_derivative: a step that does not change x taken
+    relative to x, steps turned around or shortened to stay inside the
+    bounds), and the realised steps."""
+    pts, dx = [list(x0)], []
+    for i, xi in enumerate(x0):
+        h = step
+        if (xi + h) - xi == 0.0:
+            h = eps2 * (1.0 if xi >= 0 else -1.0) * max(1.0, abs(xi))
+        lower_dist, upper_dist = xi - lb[i], ub[i] - xi
+        xs = xi + h
+        violated = xs < lb[i] or xs > ub[i]
+        fitting = abs(h) <= max(lower_dist, upper_dist)
+        if violated and fitting:
+            h = -h
+        elif not fitting:
+            h = upper_dist if upper_dist >= lower_dist else -lower_dist
+        x1 = list(x0)
+        x1[i] = xi + h
+        pts.append(x1)
+        dx.append((xi + h) - xi)
+    return pts, dx
 
-    def fm(x):
-        key = tuple(float(v) for v in np.asarray(x).ravel())
-        if last[0] != key:
-            last[0], last[1] = key, f(np.array(key))
-        return last[1]
-    return fm
 
-
-def _forward_difference(f, bounds, step=1e-8):
-    """The gradient L-BFGS-B estimates when no jac is given (scipy's 2-point
-    approx_derivative with absolute step ``step``, the steps turned around or
-    shortened to stay inside ``bounds``), as a jac callable: the same
-    numbers (the same float64 operations on Python floats) without the
-    general machinery's per-call overhead."""
+def _value_and_gradient(f_rows, bounds, step=1e-8):
+    """For minimize(..., jac=True): f(x) and the gradient L-BFGS-B estimates
+    when no jac is given (the 2-point forward difference above), the same
+    numbers (float64 operations on Python floats), with x and the forward
+    points evaluated together in one call ``f_rows(points)`` -> values."""
     lb = [float(b[0]) for b in bounds]
     ub = [float(b[1]) for b in bounds]
     eps2 = float(np.finfo(np.float64).eps ** 0.5)
 
-    def grad(x):
+    def fg(x):
         x0 = [float(v) for v in np.asarray(x).ravel()]
-        f0 = f(np.array(x0))
-        g = np.empty(len(x0))
-        for i, xi in enumerate(x0):
-            h = step
-            if (xi + h) - xi == 0.0:
-                h = eps2 * (1.0 if xi >= 0 else -1.0) * max(1.0, abs(xi))
-            lower_dist, upper_dist = xi - lb[i], ub[i] - xi
-            xs = xi + h
-            violated = xs < lb[i] or xs > ub[i]
-            fitting = abs(h) <= max(lower_dist, upper_dist)
-            if violated and fitting:
-                h = -h
-            elif not fitting:
-                h = upper_dist if upper_dist >= lower_dist else -lower_dist
-            x1 = list(x0)
-            x1[i] = xi + h
-            g[i] = (f(np.array(x1)) - f0) / ((xi + h) - xi)
-        return g
-    return grad
+        pts, dx = _forward_points(x0, lb, ub, step, eps2)
+        v = f_rows(np.array(pts))
+        return v[0], np.array([(v[1 + i] - v[0]) / dx[i] for i in range(len(dx))])
+    return fg
 
 
 def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
@@ -444,16 +440,16 @@ def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
     cdf = np.cumsum(hist)
     cdf /= cdf[-1]
 
-    def err(params):
-        # scipy.stats.norm.cdf(counts, loc, scale) (zorro.py:2553) evaluates
-        # ndtr((counts - loc) / scale); calling ndtr directly gives the same
-        # values without the distribution machinery's overhead
-        return np.sum(np.abs(cdf - scipy.special.ndtr((counts - params[0]) / params[1])))
+    def err_rows(P):
+        # sum |cdf - norm.cdf(counts, loc, scale)| (zorro.py:2553) for every
+        # row (loc, scale) of P; norm.cdf evaluates ndtr((counts - loc) /
+        # scale), and each row sums as a 1-D array would
+        z = (counts[None, :] - P[:, 0:1]) / P[:, 1:2]
+        return np.sum(np.abs(cdf[None, :] - scipy.special.ndtr(z)), axis=1)
 
     bounds = ((sumMean - 0.5 * poissonStd, sumMean + 0.5 * poissonStd), (0.7 * poissonStd, 1.3 * poissonStd))
-    errm = _memo_last(err)
-    best = scipy.optimize.minimize(errm, (sumMean, poissonStd), method="L-BFGS-B", bounds=bounds,
-                                   jac=_forward_difference(errm, bounds))
+    best = scipy.optimize.minimize(_value_and_gradient(err_rows, bounds), (sumMean, poissonStd), method="L-BFGS-B",
+                                   bounds=bounds, jac=True)
     with np.errstate(all="ignore"):
         sig_cdf = np.sqrt(2) * scipy.special.erfinv(2.0 * cdf - 1)
     normal = (counts - best.x[0]) / best.x[1]

@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import collections
 import concurrent.futures as cf
+import copy
 import threading
 import time
 
@@ -48,6 +49,14 @@ def movie_bytes(reg, frames_shape, raw_itemsize):
     if "dose" in filt:
         b += DOSE_WORK
     b += 256 << 20                               # FRC, peaks, small buffers
+    if getattr(reg, "doEvenOddFRC", False) and N >= 4:
+        # the even and odd halves are registered again at the same time, each
+        # on its own slot, from float32 aligned frames
+        half = copy.copy(reg)
+        half.doEvenOddFRC = False
+        half.keepAlignedImages = False
+        half.filterMode = "hot" if "hot" in filt else None
+        b += 2 * movie_bytes(half, (N // 2, H, W), 4)
     return int(b)
 
 
