@@ -306,3 +306,19 @@ def test_binned_movie_against_oracle():
     assert np.abs(reg.translations - ref["translations"]).max() <= TRAJ_TOL
     assert rel_l2(reg.imageSum, ref["imageSum"]) <= SUM_TOL
     assert rel_l2(reg.filtSum, ref["filtSum"]) <= SUM_TOL
+
+
+@pytest.mark.parametrize("shape", [(200, 180), (201, 183)])
+def test_strided_frame_selection_reads_in_place(shape):
+    """Every other frame of a device stack (how the even/odd FRC hands the
+    aligned halves on) registers exactly like its contiguous copy; the
+    201 x 183 movie's odd-frame view starts off a 16-byte boundary and is
+    copied, the 200 x 180 one is read in place through its frame stride."""
+    import torch
+    mv = make_movie(12, shape, seed=6, mean_dose=2.0, drift_sigma=0.8)
+    dev = torch.from_numpy(mv["images"]).cuda()
+    attrs = dict(triMode="tri", shapePadded=[256, 256], fouCrop=[256, 256], maxShift=16, doLazyFRC=False)
+    a = gpu_align(dev[1::2], **attrs)
+    b = gpu_align(dev[1::2].contiguous(), **attrs)
+    assert np.array_equal(a.translations, b.translations)
+    assert np.array_equal(a.imageSum, b.imageSum)

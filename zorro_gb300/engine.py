@@ -180,7 +180,14 @@ class Engine:
             raise ValueError("zorro.alignImageStack: stacks must be 3D data")
         if dt not in _RAW_TYPES:
             raise ValueError("images dtype %s not supported (float32, uint8, uint16, float16)" % dt)
-        t = t.contiguous()
+        # a selection of frames with contiguous rows (the even or odd frames of
+        # an aligned stack) is read in place through the frame stride, when
+        # its start and stride keep the kernels' 16-byte vector loads aligned
+        N_, H_, W_ = (int(v) for v in t.shape)
+        in_place = (t.is_cuda and t.stride(2) == 1 and t.stride(1) == W_ and t.stride(0) >= H_ * W_
+                    and t.stride(0) % 4 == 0 and t.data_ptr() % 16 == 0)
+        if not in_place:
+            t = t.contiguous()
         gain = None
         raw_float = bool(getattr(reg, "imagesAreRaw", False))  # float frames read by loadData, gain not applied
         if reg.gainRef is not None and (dt != np.dtype(np.float32) or raw_float):
@@ -284,7 +291,7 @@ class Engine:
         N, H, W = raw.shape
         return Frames(raw.data_ptr(), rtype, gain.data_ptr() if gain is not None else None,
                       ha.data_ptr() if ha is not None else None, hb.data_ptr() if hb is not None else None,
-                      float(gdiv), N, H, W, 0)
+                      float(gdiv), N, H, W, int(raw.stride(0)))
 
     def _cropped_peaks(self, reg, pairs, refine, N, C0, C1, mS, pp, spec, st):
         """The +/-maxShift correlation windows of every pair (mnxc2,
