@@ -114,3 +114,78 @@ def test_fourier_binning_matches_oracle(shape, binned):
     got = out.cpu().numpy()
     err = np.abs(got - ref).max() / np.abs(ref).max()
     assert err < 2e-5, err
+
+
+def _stream():
+    import ctypes
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def test_histogram_matches_numpy():
+    """zr_histogram against np.histogram (hotpixFilter's histogram,
+    zorro.py:2530-2533): unit bins from a half-integer edge (float32 path)
+    and from another edge (float64 path), values on and next to every edge."""
+    import torch
+    from zorro_gb300 import _lib
+    rng = np.random.default_rng(5)
+    v = rng.poisson(20.0, 300000).astype(np.float32) * rng.uniform(0.9, 1.1, 300000).astype(np.float32)
+    extra = []
+    for h in np.arange(-3.5, 60.5, 0.5, dtype=np.float32):
+        extra += [h, np.nextafter(h, np.float32(-np.inf)), np.nextafter(h, np.float32(np.inf))]
+    extra += [-1e-30, -0.0, 0.0, np.inf, -np.inf, np.nan, 3e9, -0.50000006, -0.49999997]
+    v = np.concatenate([v, np.array(extra, np.float32)])
+    dv = torch.from_numpy(v).cuda()
+    for e0, nb in [(-0.5, 45), (4.5, 40), (0.25, 50)]:
+        edges = e0 + np.arange(nb + 1, dtype=np.float64)
+        want, _ = np.histogram(v[np.isfinite(v)], edges)
+        h = torch.zeros(nb, dtype=torch.int32, device="cuda")
+        _lib.call("zr_histogram", dv.data_ptr(), v.size, e0, nb, h.data_ptr(), _stream())
+        assert np.array_equal(h.cpu().numpy(), want), e0
+
+
+def test_hotpix_maps_match_oracle():
+    """zr_hotpix_maps on the oracle's unaligned sum with the oracle's fit:
+    dead/hot/neighbourly counts exact; logisticMask and the fill map
+    (singleton PSF fill + neighbourFilt) within float32 rounding.  The movie
+    has a dead strip on the top rows and the right columns and a hot cluster,
+    so that many pixels take the neighbour branch (also at the edges)."""
+    import torch
+    from zorro_gb300 import _lib
+    from zorro_gb300._lib import HotpixParams
+    mv = make_movie(12, (203, 190), seed=9, mean_dose=2.0, drift_sigma=0.5, dtype="uint8", gain_map=True,
+                    hot_fraction=3e-3)
+    imgs = mv["images"].copy()
+    imgs[:, :3, :] = 0.0
+    imgs[:, :, -2:] = 0.0
+    imgs[:, 100:105, 40:46] *= 8.0
+    info0 = dict(zo.DEFAULTS["hotpixInfo"])
+    _, info, maps = zo.hotpix_filter(imgs.copy(), info0, dt=zo.Dtypes(True))
+    usum = maps["unalignedSum"].astype(np.float32)
+    fit = maps["fit"]
+    m, H, W = imgs.shape
+    prm = HotpixParams()
+    prm.mu, prm.sigma = float(fit["mu"]), float(fit["sigma"])
+    prm.cutoff_lower, prm.cutoff_upper = float(fit["cutoffLower"]), float(fit["cutoffUpper"])
+    prm.logistic_k, prm.relax = float(np.float32(info0["logisticK"])), float(np.float32(info0["relax"]))
+    psf = zo.psf_kernel("K2", zo.Dtypes(True)).ravel()
+    for i in range(9):
+        prm.psf[i] = float(psf[i])
+    prm.neighbour_thres = 0.01
+    prm.best_mean = float(fit["mu"] / m)
+    lib = _lib.load()
+    du = torch.from_numpy(usum).cuda()
+    ha = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    hb = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    cnt = torch.zeros(4, dtype=torch.int32, device="cuda")
+    wb = lib.zr_hotpix_work_bytes(H, W)
+    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+    import ctypes
+    _lib.call("zr_hotpix_maps", du.data_ptr(), H, W, m, ctypes.byref(prm), ha.data_ptr(), hb.data_ptr(),
+              cnt.data_ptr(), work.data_ptr(), wb, _stream())
+    c = cnt.cpu().numpy()
+    assert (int(c[0]), int(c[1]), int(c[2])) == (info["guessDeadpix"], info["guessHotpix"], info["neighborPix"])
+    assert info["neighborPix"] > 500 and info["guessDeadpix"] > 500
+    np.testing.assert_allclose(ha.cpu().numpy(), maps["logisticMask"], rtol=0, atol=2e-6)
+    b_ref = maps["singleton"] * maps["psfFiltMean"] + maps["neighbourFilt"]
+    np.testing.assert_allclose(hb.cpu().numpy(), b_ref, rtol=0, atol=2e-6 * max(1.0, float(np.abs(b_ref).max())))
