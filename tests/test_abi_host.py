@@ -70,6 +70,39 @@ def test_shift_kernels_match_reference_kernel():
             np.testing.assert_allclose(np.outer(ky, kx), k2, rtol=1e-12, atol=1e-15)
 
 
+def test_shift_table_matches_per_frame_records():
+    """shift_table (all frames at once) gives the bytes of the zr_shift_t
+    records built frame by frame from shift_params, for float64, float32 and
+    integer translations, and for the integer-roll-only case."""
+    import ctypes
+    from zorro_gb300._lib import Shift
+    assert hm.SHIFT_DTYPE.itemsize == ctypes.sizeof(Shift)
+    rng = np.random.default_rng(2)
+    H, W = 3838, 3710
+    for trial in range(60):
+        n = int(rng.integers(1, 50))
+        t = rng.normal(0, 5, (n, 2))
+        if trial % 3 == 0:
+            t = np.round(t * 16) / 16
+        if trial % 4 == 0:
+            t[::3] = np.round(t[::3])
+        if trial % 5 == 0:
+            t = t.astype(np.float32)
+        if trial % 7 == 0:
+            t = np.round(t).astype(int)
+        sh = (Shift * n)()
+        for k, (ry, rx, ap, ky, kx) in enumerate(hm.shift_params(t)):
+            sh[k].roll_y, sh[k].roll_x, sh[k].apply = ry % H, rx % W, ap
+            for i in range(3):
+                sh[k].ky[i] = float(ky[i])
+                sh[k].kx[i] = float(kx[i])
+        assert bytes(sh) == hm.shift_table(t, H, W).tobytes(), trial
+        rolls = hm.shift_table(t, H, W, lanczos=False)
+        assert np.array_equal(rolls["roll_y"], np.round(t[:, 0]).astype(int) % H)
+        assert np.array_equal(rolls["roll_x"], np.round(t[:, 1]).astype(int) % W)
+        assert not rolls["apply"].any() and (rolls["ky"] == [0, 1, 0]).all() and (rolls["kx"] == [0, 1, 0]).all()
+
+
 def test_frc_tiles_match_oracle():
     rng = np.random.default_rng(1)
     for shape in ((800, 800), (3838, 3710), (1024, 1024)):

@@ -31,7 +31,7 @@ import numpy as np
 
 from . import _lib
 from . import hostmath as hm
-from ._lib import Frames, HotpixParams, PeakParams, PeakResult, Shift, DoseParams
+from ._lib import Frames, HotpixParams, PeakParams, PeakResult, DoseParams
 
 # host view of zr_peak_result_t
 _PEAK_DTYPE = np.dtype([("sy", "f8"), ("sx", "f8"), ("sigma", "f8"), ("corr", "f4"), ("peaksig", "f4"),
@@ -108,14 +108,16 @@ class Engine:
         return {k: sum(a.elapsed_time(b) for a, b in v) for k, v in (self.profile or {}).items()}
 
     # ------------------------------------------------------------------ slots and buffers
-    def _slot(self, slot):
+    def _slot(self, slot, priority=0):
         """Per-slot state: a buffer pool and (except slot 0, which uses the
-        caller's current stream) a stream of its own.  Movies registered in
-        different slots can run concurrently from different threads."""
+        caller's current stream) a stream of its own, made with ``priority``
+        (negative: ahead of the other streams' kernels) on first use.  Movies
+        registered in different slots can run concurrently from different
+        threads."""
         with self._slots_lock:
             st = self._slots.get(slot)
             if st is None:
-                stream = None if slot == 0 else self.torch.cuda.Stream(device=self.dev)
+                stream = None if slot == 0 else self.torch.cuda.Stream(device=self.dev, priority=priority)
                 st = self._slots[slot] = {"bufs": {}, "stream": stream, "key": slot}
             return st
 
@@ -240,7 +242,7 @@ class Engine:
             ready.record()
         parent = self._tls.slot["key"]
 
-        def register(images, sub_slot, **kw):
+        def register(images, sub_slot, after_hot=None, start=None, **kw):
             r = ImageRegistrator()
             copy_config(reg, r)
             r.images = images
@@ -257,16 +259,29 @@ class Engine:
             r.bench = {}
             for k, v in kw.items():
                 setattr(r, k, v)
-            self._slot(sub_slot)["stream"].wait_event(ready)
-            self.align(r, slot=sub_slot)
+            if start is not None:
+                start.wait()
+            # the half sets are on the critical path, the parent's dose filter
+            # is not: their streams go first and the dose fills the gaps
+            self._slot(sub_slot, priority=-1)["stream"].wait_event(ready)
+            self._tls.after_hot = after_hot
+            try:
+                self.align(r, slot=sub_slot)
+            finally:
+                self._tls.after_hot = None
             return r
 
         # the two halves are independent: the odd one on a second slot (its own
-        # stream and buffers) in a helper thread, so that one half's host steps
-        # (hot-pixel fit, drift solve) overlap the other's kernels
+        # stream and buffers) in a helper thread, started once the even one has
+        # passed its hot-pixel fit, so that each half's host steps (hot-pixel
+        # fit, drift solve) overlap the other's kernels instead of each other
+        go = threading.Event()
         with concurrent.futures.ThreadPoolExecutor(1) as ex:
-            fut = ex.submit(register, aligned[1::2], ("halfset_odd", parent))
-            ev = register(aligned[0::2], ("halfset_even", parent))
+            fut = ex.submit(register, aligned[1::2], ("halfset_odd", parent), start=go)
+            try:
+                ev = register(aligned[0::2], ("halfset_even", parent), after_hot=go.set)
+            finally:
+                go.set()  # also when the even half failed before its hot-pixel step
             od = fut.result()
         eo = register(torch.stack([ev.imageSum, od.imageSum]), ("halfset_even", parent), triMode="first",
                       keepAlignedImages=True)
@@ -565,6 +580,10 @@ class Engine:
             hotinfo["frameStd"] = float(sg / np.sqrt(N))
             frames = self._frames(raw, rtype, gain, ha, hb, gdiv)
             bench["hot1"] = time.time()
+        hook = getattr(self._tls, "after_hot", None)
+        if hook is not None:
+            self._tls.after_hot = None
+            hook()
 
         # ---- padding and crop sizes (padStack zorro.py:1908, __init_xcorrnm2 zorro.py:598-611)
         if reg.shapePadded is not None and np.any(reg.shapePadded):
@@ -737,27 +756,21 @@ class Engine:
         # ---- shifts and sums (applyShifts zorro.py:1734-1808)
         if reg.originMode == "centroid":
             translations = translations - np.mean(translations, axis=0)
-        if not (reg.subPixReg > 1.0 and reg.shiftMethod == "lanczos"):
-            # integer roll only (zorro.py:1790-1796)
-            params = [(int(v[0]), int(v[1]), 0, np.array([0, 1.0, 0]), np.array([0, 1.0, 0]))
-                      for v in np.round(translations).astype(int)]
-        else:
-            params = hm.shift_params(translations)
-        sh = (Shift * N)()
-        for n, (ry, rx, ap, ky, kx) in enumerate(params):
-            sh[n].roll_y, sh[n].roll_x, sh[n].apply = ry % H, rx % W, ap
-            for i in range(3):
-                sh[n].ky[i] = float(ky[i])
-                sh[n].kx[i] = float(kx[i])
-        sh_dev = torch.frombuffer(bytearray(bytes(sh)), dtype=torch.uint8).to(self.dev, non_blocking=True)
+        # integer roll only unless subPixReg > 1 with 'lanczos' (zorro.py:1790-1796)
+        tab = hm.shift_table(translations, H, W, lanczos=reg.subPixReg > 1.0 and reg.shiftMethod == "lanczos")
+        sh_dev = torch.from_numpy(tab.view(np.uint8)).to(self.dev, non_blocking=True)
         isum = self.tensor("isum", (H, W), torch.float32)
-        esum = self.tensor("esum", (H, W), torch.float32)
-        osum = self.tensor("osum", (H, W), torch.float32)
+        # the even/odd half sums feed only the lazy FRC (the independent
+        # even/odd FRC registers the halves again)
+        lazy = bool(reg.doLazyFRC) and not reg.doEvenOddFRC
+        esum = self.tensor("esum", (H, W), torch.float32) if lazy else None
+        osum = self.tensor("osum", (H, W), torch.float32) if lazy else None
         need_aligned = (reg.keepAlignedImages or bool(reg.doEvenOddFRC) or
                         any(f in ("dose", "dosenorm") for f in filt))
         aligned = self.tensor("aligned", (N, H, W), torch.float32) if need_aligned else None
-        self.call("G_shift_sum", "zr_shift_sum", C.byref(frames), sh_dev.data_ptr(), isum.data_ptr(), esum.data_ptr(),
-                  osum.data_ptr(), aligned.data_ptr() if aligned is not None else None, st)
+        self.call("G_shift_sum", "zr_shift_sum", C.byref(frames), sh_dev.data_ptr(), isum.data_ptr(),
+                  esum.data_ptr() if lazy else None, osum.data_ptr() if lazy else None,
+                  aligned.data_ptr() if aligned is not None else None, st)
         bench["shifts1"] = time.time()
 
         # the aligned stack is complete here: the half-set registrations of the

@@ -315,6 +315,42 @@ def lanczos_kernel_1d(frac):
     return k / np.sum(k)
 
 
+SHIFT_DTYPE = np.dtype([("roll_y", "<i4"), ("roll_x", "<i4"), ("apply", "<i4"), ("ky", "<f4", 3), ("kx", "<f4", 3)])
+
+
+def shift_table(translations, H, W, lanczos=True):
+    """The zr_shift_t records of every frame at once (applyShifts,
+    zorro.py:1734-1808 with lanczosIndexedShift, zorro_util.py:341-379): the
+    integer roll (np.round) reduced to [0, H) x [0, W), and, with ``lanczos``,
+    the two axes of the normalised Lanczos-2 kernel of the fractional
+    remainder, skipped (apply = 0) when both remainders are close to zero.
+    The same operations per frame as shift_params, on arrays."""
+    t = np.asarray(translations).reshape(-1, 2)
+    if not np.issubdtype(t.dtype, np.floating):
+        t = t.astype(np.float64)  # float32 translations keep their precision, as in the reference
+    out = np.zeros(len(t), dtype=SHIFT_DTYPE)
+    it = np.round(t).astype(int)
+    out["roll_y"] = np.mod(it[:, 0], H)
+    out["roll_x"] = np.mod(it[:, 1], W)
+    ident = np.array([0.0, 1.0, 0.0])
+    if not lanczos:
+        out["ky"] = ident
+        out["kx"] = ident
+        return out
+    rem = np.remainder(t, 1)
+    apply = ~(np.isclose(rem[:, 0], 0.0) & np.isclose(rem[:, 1], 0.0))
+    base = np.arange(-1.5, 1.5) + 1.0
+
+    def kern(frac):
+        u = (2.0 / 3.0) * (base[None, :] - frac[:, None])
+        k = np.sinc(u * 2.0) * np.sinc(u)
+        return k / np.sum(k, axis=1, keepdims=True)
+    out["apply"] = apply
+    out["ky"] = np.where(apply[:, None], kern(rem[:, 0]), ident[None, :])
+    out["kx"] = np.where(apply[:, None], kern(rem[:, 1]), ident[None, :])
+    return out
+
+
 def shift_params(translations):
     """Per-frame roll and sub-pixel kernel of applyShifts with
     shiftMethod='lanczos'.  zorro_util.py:341-379."""
