@@ -70,8 +70,8 @@ def algorithmic_bytes(N, H, W, C, w, M, b_in, evenodd=False, hot=True):
     every output written once (FFT intermediates excluded).  With ``evenodd``
     the two half-set registrations of the independent FRC (n = N/2 aligned
     float32 frames each, hot filter, spectra, terms, the half triangle,
-    shift-sum) and the 'first' alignment of the two sums are added to the
-    stages they run in."""
+    shift-sum) and the 'first' alignment of the two sums (with its own hot
+    filter) are added to the stages they run in."""
     HW = H * W
     spec = C * (C // 2 + 1) * 8
 
@@ -84,7 +84,7 @@ def algorithmic_bytes(N, H, W, C, w, M, b_in, evenodd=False, hot=True):
     ab["I_dose"] = N * HW * b_in + 16 * HW
     if evenodd:
         n = N // 2
-        for part in (one(n, n * (n - 1) // 2, 4, hot), one(n, n * (n - 1) // 2, 4, hot), one(2, 1, 4, False)):
+        for part in (one(n, n * (n - 1) // 2, 4, hot), one(n, n * (n - 1) // 2, 4, hot), one(2, 1, 4, hot)):
             for k, v in part.items():
                 ab[k] += v
     return ab

@@ -96,3 +96,33 @@ def test_admission_under_a_small_budget():
             _compare(r, res[0])
     finally:
         srv.close()
+
+
+def test_even_odd_frc_alone_and_served():
+    """The independent even/odd FRC runs its half-set registrations on streams
+    of their own, ahead of the parent's dose filter: the same results alone
+    and with two movies in flight."""
+    from zorro_gb300.serve import MovieServer
+    mk = dict(n_frames=24, shape=(1100, 1080), seed=41, mean_dose=1.2, drift_sigma=0.9, dtype="uint8",
+              gain_map=True, hot_fraction=1e-3)
+    attrs = dict(triMode="tri", shapePadded=[2048, 2048], fouCrop=[512, 512], maxShift=20, pixelsize=0.1,
+                 filterMode="hot,dose", doseFiltParam=DOSE, doEvenOddFRC=True)
+    mv = make_movie(**mk)
+    alone = _reg(mk, attrs, mv)
+    alone.alignImageStack()
+    assert not np.all(np.isnan(alone.FRC))
+    other = MIX[1]
+    omv = make_movie(**other[0])
+    srv = MovieServer(slots=2, hbm_budget=40e9)
+    try:
+        futs = [srv.submit(_reg(mk, attrs, mv)), srv.submit(_reg(other[0], other[1], omv)),
+                srv.submit(_reg(mk, attrs, mv))]
+        for f in (futs[0], futs[2]):
+            r = f.result(timeout=600)
+            _compare(r, alone)
+            assert np.abs(np.asarray(r.transEven) - np.asarray(alone.transEven)).max() <= 1e-9
+            assert np.abs(np.asarray(r.transOdd) - np.asarray(alone.transOdd)).max() <= 1e-9
+            assert np.array_equal(np.isnan(np.asarray(r.FRC)), np.isnan(np.asarray(alone.FRC)))
+        futs[1].result(timeout=600)
+    finally:
+        srv.close()

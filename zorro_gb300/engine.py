@@ -283,8 +283,12 @@ class Engine:
             finally:
                 go.set()  # also when the even half failed before its hot-pixel step
             od = fut.result()
-        eo = register(torch.stack([ev.imageSum, od.imageSum]), ("halfset_even", parent), triMode="first",
-                      keepAlignedImages=True)
+        # the half sums are complete (each half-set stream was synchronised):
+        # stack them on the stream that registers the pair, not on the parent's,
+        # whose low-priority dose kernels may still be queued ahead of the copy
+        with torch.cuda.stream(self._slot(("halfset_even", parent), priority=-1)["stream"]):
+            pair = torch.stack([ev.imageSum, od.imageSum])
+        eo = register(pair, ("halfset_even", parent), triMode="first", keepAlignedImages=True)
         te, to = np.asarray(ev.translations), np.asarray(od.translations)
         box = 512
         offs, tiles = hm.frc_tiles((H, W), np.hstack([te, to]))
