@@ -322,3 +322,26 @@ def test_strided_frame_selection_reads_in_place(shape):
     b = gpu_align(dev[1::2].contiguous(), **attrs)
     assert np.array_equal(a.translations, b.translations)
     assert np.array_equal(a.imageSum, b.imageSum)
+
+
+@pytest.mark.parametrize("dtype,shape", [("uint16", (300, 290)), ("float16", (301, 291)), ("uint8", (301, 291))])
+def test_raw_counts_with_gain_equal_corrected_frames(dtype, shape):
+    """Raw detector counts (uint8 / uint16 / float16) with gainRef give the
+    same registration, bit for bit, as the float32 frames float32(gain * raw)
+    (loadData's gain multiply, zorro.py:3466, fused into every frame read):
+    hot-pixel counts, trajectory, sums, FRC."""
+    mv = make_movie(10, shape, seed=13, mean_dose=1.5, drift_sigma=0.8, dtype="uint8", gain_map=True,
+                    hot_fraction=1e-3)
+    raw = mv["raw"].astype(dtype)
+    gain = mv["gain"].astype(np.float32)
+    frames = (gain[None, :, :] * raw.astype(np.float32)).astype(np.float32)
+    attrs = dict(triMode="tri", shapePadded=[512, 512], fouCrop=[256, 256], maxShift=20, pixelsize=0.1,
+                 filterMode="hot,dose", doseFiltParam=DOSE)
+    a = gpu_align(raw, gain=gain, **attrs)
+    b = gpu_align(frames, **attrs)
+    for k in ("guessDeadpix", "guessHotpix", "neighborPix"):
+        assert a.hotpixInfo[k] == b.hotpixInfo[k], k
+    assert np.array_equal(a.translations, b.translations)
+    assert np.array_equal(a.imageSum, b.imageSum)
+    assert np.array_equal(a.filtSum, b.filtSum)
+    assert np.array_equal(np.asarray(a.FRC), np.asarray(b.FRC), equal_nan=True)

@@ -189,3 +189,39 @@ def test_hotpix_maps_match_oracle():
     np.testing.assert_allclose(ha.cpu().numpy(), maps["logisticMask"], rtol=0, atol=2e-6)
     b_ref = maps["singleton"] * maps["psfFiltMean"] + maps["neighbourFilt"]
     np.testing.assert_allclose(hb.cpu().numpy(), b_ref, rtol=0, atol=2e-6 * max(1.0, float(np.abs(b_ref).max())))
+
+
+@pytest.mark.parametrize("rtype,shape", [(0, (64, 60)), (1, (64, 60)), (2, (64, 60)), (3, (64, 60)),
+                                         (1, (63, 61)), (2, (65, 59)), (3, (63, 61))])
+@pytest.mark.parametrize("gdiv", [0.0, 3.0])
+def test_gain_sum_every_raw_type(rtype, shape, gdiv):
+    """zr_gain_sum against the frame-ordered float32 sum of
+    float32(gain * raw) (/ gdiv): every raw type, the vector path (H*W % 4 ==
+    0) and the per-pixel path; the float64 total within rounding."""
+    import ctypes
+    import torch
+    from zorro_gb300 import _lib
+    from zorro_gb300._lib import Frames
+    rng = np.random.default_rng(rtype * 10 + shape[1])
+    N, (H, W) = 11, shape
+    np_t = {0: np.float32, 1: np.uint8, 2: np.uint16, 3: np.float16}[rtype]
+    raw = rng.poisson(3.0, (N, H, W)).astype(np_t)
+    if rtype in (0, 3):
+        raw = (raw + rng.uniform(0, 1, (N, H, W))).astype(np_t)
+    gain = rng.uniform(0.8, 1.2, (H, W)).astype(np.float32)
+    want = np.zeros((H, W), np.float32)
+    for n in range(N):
+        v = gain * raw[n].astype(np.float32)
+        if gdiv:
+            v = v / np.float32(gdiv)
+        want = want + v
+    draw = torch.from_numpy(raw.view(np.int16) if rtype == 2 else raw).cuda()  # the same bytes
+    dgain = torch.from_numpy(gain).cuda()
+    fr = Frames()
+    fr.raw, fr.raw_type, fr.gain, fr.hot_a, fr.hot_b = draw.data_ptr(), rtype, dgain.data_ptr(), None, None
+    fr.gain_divisor, fr.n_frames, fr.height, fr.width, fr.frame_stride = gdiv, N, H, W, H * W
+    out = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+    tot = torch.zeros(1, dtype=torch.float64, device="cuda")
+    _lib.call("zr_gain_sum", ctypes.byref(fr), out.data_ptr(), tot.data_ptr(), _stream())
+    assert np.array_equal(out.cpu().numpy(), want)
+    assert abs(tot.item() - want.astype(np.float64).sum()) <= 1e-9 * abs(want.astype(np.float64).sum())
