@@ -33,38 +33,6 @@ __global__ void k_gain_sum(FrameSrc f, float* __restrict__ sum, double* __restri
   }
 }
 
-// Raw bits of the four consecutive pixels at element i (u8 in .x, u16/f16
-// in .x/.y, f32 in .x-.w) and their values.
-template <int TYPE>
-__device__ __forceinline__ uint4 raw_quad(const void* raw, long long i) {
-  uint4 r = make_uint4(0u, 0u, 0u, 0u);
-  if (TYPE == ZR_U8) {
-    r.x = __ldg(reinterpret_cast<const unsigned int*>((const uint8_t*)raw + i));
-  } else if (TYPE == ZR_U16 || TYPE == ZR_F16) {
-    const uint2 v = __ldg(reinterpret_cast<const uint2*>((const uint16_t*)raw + i));
-    r.x = v.x;
-    r.y = v.y;
-  } else {
-    r = __ldg(reinterpret_cast<const uint4*>((const float*)raw + i));
-  }
-  return r;
-}
-
-template <int TYPE>
-__device__ __forceinline__ float4 quad_value(const uint4 r) {
-  if (TYPE == ZR_U8)
-    return make_float4((float)(r.x & 0xffu), (float)((r.x >> 8) & 0xffu), (float)((r.x >> 16) & 0xffu),
-                       (float)(r.x >> 24));
-  if (TYPE == ZR_U16)
-    return make_float4((float)(r.x & 0xffffu), (float)(r.x >> 16), (float)(r.y & 0xffffu), (float)(r.y >> 16));
-  if (TYPE == ZR_F16)
-    return make_float4(__half2float(__ushort_as_half((unsigned short)(r.x & 0xffffu))),
-                       __half2float(__ushort_as_half((unsigned short)(r.x >> 16))),
-                       __half2float(__ushort_as_half((unsigned short)(r.y & 0xffffu))),
-                       __half2float(__ushort_as_half((unsigned short)(r.y >> 16))));
-  return make_float4(__uint_as_float(r.x), __uint_as_float(r.y), __uint_as_float(r.z), __uint_as_float(r.w));
-}
-
 // Same sum, four pixels per thread (H*W % 4 == 0, aligned vector loads), the
 // frames read GS_FRAMES at a time before any is added, so that each thread
 // keeps that many loads in flight; the additions stay in frame order.
