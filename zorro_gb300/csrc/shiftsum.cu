@@ -34,6 +34,11 @@ __device__ __forceinline__ float raw_at(const void* raw, long long idx) {
 // running sums live in shared memory, which leaves the registers for the
 // loads in flight at eight resident CTAs per SM.
 //
+// Each thread filters four rows of one column: the six horizontal 3-tap
+// results it needs are computed once and slid down its rows for the vertical
+// taps (the same products and sums as tap by tap).  The even and odd sums are
+// kept only with HALVES (the lazy FRC reads them).
+//
 // With VEC (arrays aligned for vector loads), a frame whose 66 source columns
 // of this tile are one contiguous run (the tile away from the left and right
 // edges and the roll not wrapping inside it: nearly every tile) is read in
@@ -57,17 +62,20 @@ __device__ __forceinline__ float corrected_at(const FrameSrc& f, long long fo, l
   return v;
 }
 
-template <int TYPE, bool VEC>
+template <int TYPE, bool VEC, bool HALVES>
 __global__ void __launch_bounds__(SS_THR, ZR_SS_MINB)
     k_shift_sum(FrameSrc f, const zr_shift_t* __restrict__ sh, float* __restrict__ sum,
                 float* __restrict__ even, float* __restrict__ odd, float* __restrict__ aligned) {
   __shared__ float tile[SS_TH][SS_TW];
-  __shared__ float acc[3][SS_TY][SS_TX];  // all frames, even frames, odd frames
+  __shared__ float acc[HALVES ? 3 : 1][SS_TY][SS_TX];  // all frames (, even frames, odd frames)
   const int x0 = blockIdx.x * SS_TX, y0 = blockIdx.y * SS_TY;
   const int tx = threadIdx.x & (SS_TX - 1), ty = threadIdx.x / SS_TX;  // ty in [0,4)
   constexpr int RPT = SS_TY / (SS_THR / SS_TX);                            // rows per thread (4)
 #pragma unroll
-  for (int i = 0; i < RPT; i++) acc[0][ty * RPT + i][tx] = acc[1][ty * RPT + i][tx] = acc[2][ty * RPT + i][tx] = 0.0f;
+  for (int i = 0; i < RPT; i++) {
+    acc[0][ty * RPT + i][tx] = 0.0f;
+    if (HALVES) acc[1][ty * RPT + i][tx] = acc[2][ty * RPT + i][tx] = 0.0f;
+  }
   const int H = f.H, W = f.W;
   constexpr int TE = SS_TH * SS_TW;
   const bool x_inside = x0 >= 1 && x0 + SS_TX + 1 <= W;  // halo columns x0-1 .. x0+64 all in [0, W)
@@ -176,25 +184,29 @@ __global__ void __launch_bounds__(SS_THR, ZR_SS_MINB)
     }
     __syncthreads();
     if (n + 1 < f.N) fetch(n + 1);
-    const int x = x0 + tx;
-    float* const half_acc = acc[1 + (n & 1)][0];
+    const int x = x0 + tx, ly0 = ty * RPT;
+    float* const arow = aligned ? aligned + (size_t)n * H * W : nullptr;
+    auto emit = [&](int i, float a) {
+      const int y = y0 + ly0 + i;
+      acc[0][ly0 + i][tx] += a;
+      if (HALVES) acc[1 + (n & 1)][ly0 + i][tx] += a;
+      if (arow && y < H && x < W) arow[(size_t)y * W + x] = a;
+    };
+    if (t.apply) {
+      auto hrow = [&](int r) {
+        return fmaf(t.kx[0], tile[r][tx + 2], fmaf(t.kx[1], tile[r][tx + 1], t.kx[2] * tile[r][tx]));
+      };
+      float h0 = hrow(ly0), h1 = hrow(ly0 + 1);
 #pragma unroll
-    for (int i = 0; i < RPT; i++) {
-      const int y = y0 + ty * RPT + i;
-      float a;
-      const int ly = ty * RPT + i + 1, lx = tx + 1;
-      if (t.apply) {
-        // sum_a ky[a] sum_b kx[b] R(y - a + 1, x - b + 1)
-        float r0 = fmaf(t.kx[0], tile[ly + 1][lx + 1], fmaf(t.kx[1], tile[ly + 1][lx], t.kx[2] * tile[ly + 1][lx - 1]));
-        float r1 = fmaf(t.kx[0], tile[ly][lx + 1], fmaf(t.kx[1], tile[ly][lx], t.kx[2] * tile[ly][lx - 1]));
-        float r2 = fmaf(t.kx[0], tile[ly - 1][lx + 1], fmaf(t.kx[1], tile[ly - 1][lx], t.kx[2] * tile[ly - 1][lx - 1]));
-        a = fmaf(t.ky[0], r0, fmaf(t.ky[1], r1, t.ky[2] * r2));
-      } else {
-        a = tile[ly][lx];
+      for (int i = 0; i < RPT; i++) {
+        const float h2 = hrow(ly0 + i + 2);
+        emit(i, fmaf(t.ky[0], h2, fmaf(t.ky[1], h1, t.ky[2] * h0)));
+        h0 = h1;
+        h1 = h2;
       }
-      acc[0][ly - 1][tx] += a;
-      half_acc[(ly - 1) * SS_TX + tx] += a;
-      if (aligned && y < H && x < W) aligned[(size_t)n * H * W + (size_t)y * W + x] = a;
+    } else {
+#pragma unroll
+      for (int i = 0; i < RPT; i++) emit(i, tile[ly0 + i + 1][tx + 1]);
     }
   }
   const int x = x0 + tx;
@@ -204,8 +216,10 @@ __global__ void __launch_bounds__(SS_THR, ZR_SS_MINB)
     if (y < H && x < W) {
       const size_t p = (size_t)y * W + x;
       sum[p] = acc[0][ty * RPT + i][tx];
-      if (even) even[p] = acc[1][ty * RPT + i][tx];
-      if (odd) odd[p] = acc[2][ty * RPT + i][tx];
+      if (HALVES) {
+        if (even) even[p] = acc[1][ty * RPT + i][tx];
+        if (odd) odd[p] = acc[2][ty * RPT + i][tx];
+      }
     }
   }
 }
@@ -226,9 +240,12 @@ extern "C" int zr_shift_sum(const zr_frames_t* frames, const zr_shift_t* shifts,
   const int qbytes = f.type == ZR_U8 ? 4 : (f.type == ZR_F32 ? 16 : 8);
   const bool vec = f.fstride % 4 == 0 && ((uintptr_t)f.raw % qbytes) == 0 && ((uintptr_t)f.gain & 15) == 0 &&
                    ((uintptr_t)f.ha & 15) == 0 && ((uintptr_t)f.hb & 15) == 0;
-#define ZR_SS_LAUNCH(T)                                                                                        \
-  (vec ? k_shift_sum<T, true><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned)      \
-       : k_shift_sum<T, false><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned))
+  const bool halves = even_sum || odd_sum;
+#define ZR_SS_LAUNCH(T)                                                                                             \
+  (vec ? (halves ? k_shift_sum<T, true, true><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned)   \
+                 : k_shift_sum<T, true, false><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned)) \
+       : (halves ? k_shift_sum<T, false, true><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned)  \
+                 : k_shift_sum<T, false, false><<<grid, SS_THR, 0, st>>>(f, shifts, image_sum, even_sum, odd_sum, aligned)))
   switch (f.type) {
     case ZR_U8: ZR_SS_LAUNCH(ZR_U8); break;
     case ZR_U16: ZR_SS_LAUNCH(ZR_U16); break;
