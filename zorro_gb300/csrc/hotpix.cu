@@ -125,26 +125,38 @@ __global__ void k_histogram_half(const float* __restrict__ v, long long n, int k
 }
 
 // logisticMask (written as the map a) and 1 - logisticMask; dead/hot counts.
-// sigma = (s - mu) / sigma_fit enters the two logistic exponents as
-// (s - mu) * (1 / sigma_fit) in float64 (within one unit in the last place of
-// the quotient; the exponents are rounded to float32 anyway).  The counts
-// compare the float32 sum with s_dead / s_hot, the float32 values where the
-// float64 quotient crosses the cut-offs (found on the host with the same
-// float64 operations), which gives the counts of the quotient itself without
-// a float64 division per pixel.
+// The logistic exponents K (sigma - c relax), sigma = (s - mu) / sigma_fit,
+// are evaluated in float64 as one fused multiply-add each, A s + Cc with
+// A = K / sigma_fit and Cc = -K c relax - A mu folded on the host (within a
+// few units in the last float64 place of the step-by-step value; the
+// exponents are rounded to float32), or step by step as K ((s - mu) rsig -
+// c relax) when sigma_fit is 0.  The counts compare the float32 sum with
+// s_dead / s_hot, the float32 values where the float64 quotient crosses the
+// cut-offs (found on the host with the same float64 operations), which gives
+// the counts of the quotient itself without a float64 division per pixel.
 __global__ void __launch_bounds__(256) k_hot_lm(const float* __restrict__ sum, long long npix, zr_hotpix_params_t p,
-                                                double rsig, float s_dead, float s_hot, float* __restrict__ LM,
-                                                float* __restrict__ CONV, unsigned int* __restrict__ counts) {
+                                                double rsig, double A, double C1, double C2, float s_dead, float s_hot,
+                                                float* __restrict__ LM, float* __restrict__ CONV,
+                                                unsigned int* __restrict__ counts) {
   unsigned int dead = 0, hot = 0;
   const double lrel = (double)(p.cutoff_lower * p.relax), urel = (double)(p.cutoff_upper * p.relax);
   const double K = (double)p.logistic_k;
+  const bool folded = rsig < INFINITY;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < npix; i += (long long)gridDim.x * blockDim.x) {
     const float s = sum[i];
     dead += s < s_dead;
     hot += s >= s_hot;
-    const double sg = ((double)s - p.mu) * rsig;
-    const float e1 = expf((float)(K * (sg - lrel)));
-    const float e2 = expf((float)(K * (sg - urel)));
+    float x1, x2;
+    if (folded) {
+      x1 = (float)fma(A, (double)s, C1);
+      x2 = (float)fma(A, (double)s, C2);
+    } else {
+      const double sg = ((double)s - p.mu) * rsig;
+      x1 = (float)(K * (sg - lrel));
+      x2 = (float)(K * (sg - urel));
+    }
+    const float e1 = expf(x1);
+    const float e2 = expf(x2);
     const float s1 = 1.0f / (1.0f + e1);
     const float lm = (1.0f - s1) / (1.0f + e2);
     float conv;
@@ -366,12 +378,16 @@ extern "C" int zr_hotpix_maps(const float* unaligned_sum, int height, int width,
   const float s_dead = kd >= end ? INFINITY : key_value((uint32_t)kd);  // +inf: only for an infinite cut-off
   const float s_hot = kh >= end ? NAN : key_value((uint32_t)kh);         // NaN: no value is hot
   const double rsig = 1.0 / sigma;
+  const double Kd = (double)p.logistic_k;
+  const double A = Kd * rsig;
+  const double C1 = -(Kd * (double)(p.cutoff_lower * p.relax)) - A * mu;
+  const double C2 = -(Kd * (double)(p.cutoff_upper * p.relax)) - A * mu;
   const long long npix = (long long)height * width;
   float* CONV = (float*)work;
   int blocks = (int)((npix + 255) / 256);
   if (blocks > 152 * 16) blocks = 152 * 16;
   cudaStream_t st = (cudaStream_t)stream;
-  k_hot_lm<<<blocks, 256, 0, st>>>(unaligned_sum, npix, p, rsig, s_dead, s_hot, hot_a, CONV, counts3);
+  k_hot_lm<<<blocks, 256, 0, st>>>(unaligned_sum, npix, p, rsig, A, C1, C2, s_dead, s_hot, hot_a, CONV, counts3);
   ZR_TRY(launched("k_hot_lm"));
   const dim3 tiles((width + HF_TX - 1) / HF_TX, (height + HF_TY - 1) / HF_TY);
   k_hot_fill<<<tiles, 256, 0, st>>>(CONV, unaligned_sum, height, width, n_frames, p, hot_b, counts3);
