@@ -131,6 +131,14 @@ int zr_gain_sum(const zr_frames_t* frames, float* unaligned_sum, double* total, 
 int zr_histogram(const float* values, long long n, double first_edge, int nbins,
                  unsigned int* counts, void* stream);
 
+/* The float32 thresholds of the dead/hot counts (zorro.py:2595-2601): a
+ * float32 value s is counted dead when s < *s_dead and hot when s >= *s_hot,
+ * exactly when the float64 quotient (s - mu) / sigma lies below cutoff_lower
+ * or above cutoff_upper (*s_hot is NaN when no value is above).  sigma >= 0.
+ * Host code (bisection over the ordered float32 values). */
+int zr_hotpix_thresholds(double mu, double sigma, float cutoff_lower, float cutoff_upper, float* s_dead,
+                         float* s_hot);
+
 /* The logistic masks, PSF fill and neighbour fill of zorro.py:2595-2649,
  * folded into per-pixel affine maps hot_a (logisticMask) and hot_b
  * (singletonOutlierMask*psfFiltMean + neighbourFilt).  counts3 (accumulated)

@@ -50,6 +50,48 @@ def test_errors_are_reported_without_a_gpu(lib):
     assert "null" in _lib.last_error()
 
 
+def _ordered_neighbours(v, k):
+    """The k float32 values on each side of v (and v) in float32 order."""
+    u = np.array([v], np.float32).view(np.uint32)[0]
+    key = int(~u & 0xffffffff) if u & 0x80000000 else int(u | 0x80000000)
+    keys = np.arange(key - k, key + k + 1, dtype=np.int64)
+    keys = keys[(keys >= 0) & (keys <= 0xffffffff)].astype(np.uint32)
+    bits = np.where(keys & 0x80000000, keys & 0x7fffffff, ~keys).astype(np.uint32)
+    return bits.view(np.float32)
+
+
+def test_hotpix_thresholds_give_the_counts_of_the_quotient(lib):
+    """zr_hotpix_thresholds (host code of zr_hotpix_maps): counting float32
+    sums against the two float32 thresholds gives exactly the dead/hot
+    decisions of the float64 quotient (s - mu) / sigma < cutoffLower and
+    > cutoffUpper (zorro.py:2595-2601), on and around the thresholds, over a
+    sweep of values and at +-0, +-inf and NaN; sigma 0 included."""
+    import ctypes
+    from zorro_gb300 import _lib
+    rng = np.random.default_rng(6)
+    cases = [(31.396991311237343, 5.654671154694482, -4.0, 2.4724910259246826), (24.5, 0.0, -1.9, -0.25),
+             (1.0286607132473808, 1.2334786214509157, -4.0, 0.9497635), (2.5e5, 480.0, -3.3, 3.25)]
+    cases += [(float(rng.uniform(0, 100)), float(rng.uniform(0.3, 9)), float(np.float32(rng.uniform(-5, -1))),
+               float(np.float32(rng.uniform(-1, 4)))) for _ in range(20)]
+    for mu, sigma, cl, cu in cases:
+        sd, sh = ctypes.c_float(), ctypes.c_float()
+        _lib.call("zr_hotpix_thresholds", mu, sigma, cl, cu, ctypes.byref(sd), ctypes.byref(sh))
+        s_dead, s_hot = np.float32(sd.value), np.float32(sh.value)
+        vals = [_ordered_neighbours(s_dead, 3000), np.array([mu], np.float32),
+                (mu + sigma * rng.normal(0, 4, 200000)).astype(np.float32),
+                np.array([0.0, -0.0, np.inf, -np.inf, np.nan], np.float32)]
+        if np.isfinite(s_hot):
+            vals.append(_ordered_neighbours(s_hot, 3000))
+        s = np.concatenate(vals)
+        with np.errstate(all="ignore"):
+            q = (s.astype(np.float64) - mu) / sigma
+            assert np.array_equal(s < s_dead, q < np.float64(np.float32(cl))), (mu, sigma, cl)
+            assert np.array_equal(s >= s_hot, q > np.float64(np.float32(cu))), (mu, sigma, cu)
+    with pytest.raises(ValueError):
+        _lib.call("zr_hotpix_thresholds", 1.0, -1.0, -4.0, 3.0, ctypes.byref(ctypes.c_float()),
+                  ctypes.byref(ctypes.c_float()))
+
+
 @pytest.mark.parametrize("mode,w", [("tri", 5), ("diag", 3), ("diag", 1), ("first", 5), ("auto", 5)])
 def test_tri_indices_and_equation_matrix(mode, w):
     for N in (2, 7, 40):

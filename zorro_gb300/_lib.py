@@ -15,7 +15,8 @@ ZR_F32, ZR_U8, ZR_U16, ZR_F16 = 0, 1, 2, 3
 
 # every symbol the header declares
 EXPORTS = (
-    "zr_version", "zr_last_error", "zr_launch_count", "zr_init", "zr_gain_sum", "zr_histogram", "zr_hotpix_work_bytes",
+    "zr_version", "zr_last_error", "zr_launch_count", "zr_init", "zr_gain_sum", "zr_histogram", "zr_hotpix_thresholds",
+    "zr_hotpix_work_bytes",
     "zr_hotpix_maps", "zr_frame_sums", "zr_spectrum_pitch", "zr_spectrum_elems", "zr_spectra_work_bytes",
     "zr_spectra", "zr_xcorr_work_bytes", "zr_xcorr_terms", "zr_xcorr_pairs", "zr_locate_peaks",
     "zr_shift_sum", "zr_frc_work_bytes", "zr_tiled_frc", "zr_dose_work_bytes", "zr_dose_filter",
@@ -74,6 +75,8 @@ _SIGS = {
     "zr_init": (C.c_int, [C.c_int]),
     "zr_gain_sum": (C.c_int, [C.POINTER(Frames), _P, _P, _P]),
     "zr_histogram": (C.c_int, [_P, C.c_longlong, C.c_double, C.c_int, _P, _P]),
+    "zr_hotpix_thresholds": (C.c_int, [C.c_double, C.c_double, C.c_float, C.c_float, C.POINTER(C.c_float),
+                                       C.POINTER(C.c_float)]),
     "zr_hotpix_work_bytes": (C.c_size_t, [C.c_int, C.c_int]),
     "zr_hotpix_maps": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.POINTER(HotpixParams), _P, _P, _P, _P,
                                  C.c_size_t, _P]),

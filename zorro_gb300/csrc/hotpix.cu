@@ -354,6 +354,21 @@ extern "C" int zr_histogram(const float* values, long long n, double first_edge,
   return launched("k_histogram");
 }
 
+extern "C" int zr_hotpix_thresholds(double mu, double sigma, float cutoff_lower, float cutoff_upper, float* s_dead,
+                                    float* s_hot) {
+  if (!s_dead || !s_hot) return set_error(ZR_EINVAL, "zr_hotpix_thresholds: null argument");
+  if (!(sigma >= 0.0)) return set_error(ZR_EINVAL, "zr_hotpix_thresholds: sigma %g is not >= 0", sigma);
+  // sigma >= 0 makes (s - mu) / sigma monotone in s, so each cut-off test
+  // changes its answer once along the float32 values
+  const double cl = (double)cutoff_lower, cu = (double)cutoff_upper;
+  const uint64_t end = (uint64_t)order_key(INFINITY) + 1;
+  const uint64_t kd = first_false([&](float s) { return ((double)s - mu) / sigma < cl; });
+  const uint64_t kh = first_false([&](float s) { return !(((double)s - mu) / sigma > cu); });
+  *s_dead = kd >= end ? INFINITY : key_value((uint32_t)kd);  // +inf: only for an infinite cut-off
+  *s_hot = kh >= end ? NAN : key_value((uint32_t)kh);         // NaN: no value is hot
+  return ZR_OK;
+}
+
 extern "C" size_t zr_hotpix_work_bytes(int height, int width) {
   return (size_t)height * width * sizeof(float) + 256;
 }
@@ -367,16 +382,9 @@ extern "C" int zr_hotpix_maps(const float* unaligned_sum, int height, int width,
   if (work_bytes < zr_hotpix_work_bytes(height, width))
     return set_error(ZR_EWORK, "zr_hotpix_maps: work buffer too small");
   const zr_hotpix_params_t p = *params;
-  if (!(p.sigma >= 0.0)) return set_error(ZR_EINVAL, "zr_hotpix_maps: sigma %g is not >= 0", p.sigma);
-  // sigma >= 0 makes (s - mu) / sigma monotone in s, so each cut-off test
-  // changes its answer once along the float32 values
+  float s_dead = 0.0f, s_hot = 0.0f;
+  ZR_TRY(zr_hotpix_thresholds(p.mu, p.sigma, p.cutoff_lower, p.cutoff_upper, &s_dead, &s_hot));
   const double mu = p.mu, sigma = p.sigma;
-  const double cl = (double)p.cutoff_lower, cu = (double)p.cutoff_upper;
-  const uint64_t end = (uint64_t)order_key(INFINITY) + 1;
-  const uint64_t kd = first_false([&](float s) { return ((double)s - mu) / sigma < cl; });
-  const uint64_t kh = first_false([&](float s) { return !(((double)s - mu) / sigma > cu); });
-  const float s_dead = kd >= end ? INFINITY : key_value((uint32_t)kd);  // +inf: only for an infinite cut-off
-  const float s_hot = kh >= end ? NAN : key_value((uint32_t)kh);         // NaN: no value is hot
   const double rsig = 1.0 / sigma;
   const double Kd = (double)p.logistic_k;
   const double A = Kd * rsig;
