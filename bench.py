@@ -62,7 +62,28 @@ WORKLOADS = {
                              doseFiltParam=[1.0, 0.24499, -1.6649, 2.8141, 32, 0], subPixReg=16)),
 }
 METRIC = "4k x 4k x 40 movies/sec (K2 3838x3710x40 registration)"
+
 UNIT = "movies/s"
+
+
+def workload_config(name, world=1):
+    """The bench line's ``config``: the workload named by what it is, the
+    same object in both arms."""
+    wl = WORKLOADS[name]
+    mv, at = wl["movie"], wl["attrs"]
+    N, (H, W) = mv["n_frames"], mv["shape"]
+    pairs = N * (N - 1) // 2 if at["triMode"] == "tri" else None
+    desc = "%s: %dx%dx%d %s%s%s, P=%d, C=%d, %s%s, maxShift %d, %s filters" % (
+        name, N, H, W, "u8" if mv.get("dtype") == "uint8" else "f32", " + gain" if mv.get("gain_map") else "",
+        " + %g%% hot px" % (100 * mv["hot_fraction"]) if mv.get("hot_fraction") else "", at["shapePadded"][0],
+        at["fouCrop"][0], at["triMode"], " %d pairs" % pairs if pairs else "", at["maxShift"],
+        "+".join(at["filterMode"].split(",")))
+    if at.get("doEvenOddFRC"):
+        desc += ", even/odd FRC (two half-set registrations of %d frames)" % (N // 2)
+    mb = N * H * W * (1 if mv.get("dtype") == "uint8" else 4) / 1e6
+    l2 = ("inputs (%d MB raw frames per movie) larger than L2; no flush" % mb if mb > 129 else
+          "inputs (%d MB raw frames per movie) smaller than L2: a test workload, not a bench figure" % mb)
+    return {"workload": desc, "l2": l2, "parallelism": "replicas" if world > 1 else "single"}
 
 
 def algorithmic_bytes(N, H, W, C, w, M, b_in, evenodd=False, hot=True):
@@ -280,8 +301,7 @@ def run_reference(args, wl, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded K2-size movie)",
-            "config": {"workload": args.workload, **{k: wl["attrs"][k] for k in ("triMode", "shapePadded", "fouCrop",
-                                                                              "maxShift", "filterMode")}},
+            "config": workload_config(args.workload, args.gpus),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -555,11 +575,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": round(t_step * 1000.0, 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded K2-size movies)",
-                "config": {"workload": args.workload + ": 40x3838x3710 u8 + gain + 0.01% hot px, P=4096, C=2048, "
-                           "tri 780 pairs, maxShift 100, hot+dose filters, even/odd FRC (two "
-                           "half-set registrations of 20 frames)",
-                           "l2": "inputs (570 MB raw frames per movie) larger than L2; no flush",
-                           "parallelism": "replicas" if world > 1 else "single"},
+                "config": workload_config(args.workload, world),
                 "e2e": {"value": round(world / t_e2e, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
                 "served": {"value": round(world / t_served, 3), "unit": UNIT, "slots": args.slots,
