@@ -69,6 +69,12 @@ CASES = {
     "auto_mode": dict(movie=dict(n_frames=14, shape=(200, 180), seed=29, mean_dose=1.2, drift_sigma=0.8),
                       attrs=dict(triMode="auto", autoMax=6, peaksigThres=5.6, shapePadded=[256, 256],
                                  fouCrop=[128, 128], maxShift=20, pixelsize=0.1, doLazyFRC=False)),
+    # fixed Gaussian peak filter (Bmode 'conv' from Brad), peak-significance
+    # weights, 4x sub-pixel upsampling, normalised dose filter
+    "conv_corr": dict(movie=dict(n_frames=10, shape=(200, 180), seed=31, mean_dose=1.5, drift_sigma=0.8),
+                      attrs=dict(triMode="tri", shapePadded=[256, 256], fouCrop=[128, 128], maxShift=20,
+                                 pixelsize=0.1, Bmode="conv", Brad=40, weightMode="corr", subPixReg=4,
+                                 filterMode="dosenorm", doseFiltParam=DOSE, doLazyFRC=False)),
     # template mode: correlate everything to frame 0, no solver
     "first_mode": dict(movie=dict(n_frames=5, shape=(120, 128), seed=21, mean_dose=3.0, drift_sigma=1.0),
                        attrs=dict(triMode="first", shapePadded=[128, 128], fouCrop=[128, 128], maxShift=16,
