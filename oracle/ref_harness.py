@@ -55,7 +55,18 @@ import numpy as np
 import scipy.fft
 import scipy.optimize
 
-REF_ROOT = os.environ.get("ZORRO_REF_ROOT", "/root/reference")
+# The checkout of LBEM-CH/zorro to run: required, no default (the harness
+# runs only where a reference checkout exists; nothing on the GPU path does).
+REF_ROOT = os.environ.get("ZORRO_REF_ROOT")
+
+
+def ref_root():
+    """The reference checkout named by ZORRO_REF_ROOT (its zorro/zorro.py must exist)."""
+    if not REF_ROOT:
+        raise RuntimeError("set ZORRO_REF_ROOT to a checkout of LBEM-CH/zorro (the directory holding zorro/zorro.py)")
+    if not os.path.exists(os.path.join(REF_ROOT, "zorro", "zorro.py")):
+        raise RuntimeError("ZORRO_REF_ROOT=%s holds no zorro/zorro.py" % REF_ROOT)
+    return REF_ROOT
 
 # (line number, old text, new text) -- applied to the source text before
 # compiling, so reported line numbers stay those of the reference file.
@@ -230,12 +241,12 @@ def load_reference(fp64=True, workers=None):
     with _stubs_installed(workers), warnings.catch_warnings():
         warnings.simplefilter("ignore")
         util = types.ModuleType("zorro_util")
-        upath = os.path.join(REF_ROOT, "zorro", "zorro_util.py")
+        upath = os.path.join(ref_root(), "zorro", "zorro_util.py")
         util.__file__ = upath
         with open(upath) as fh:
             exec(compile(fh.read(), upath, "exec"), util.__dict__)
         sys.modules["zorro_util"] = util
-        zpath = os.path.join(REF_ROOT, "zorro", "zorro.py")
+        zpath = os.path.join(ref_root(), "zorro", "zorro.py")
         with open(zpath) as fh:
             lines = fh.read().split("\n")
         for lineno, old, new in _COMPAT_EDITS:

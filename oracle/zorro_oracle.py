@@ -635,9 +635,9 @@ def dose_filter_params(m, shapePadded, pixelsize, voltage, doseFiltParam, imageS
             "accum": accum, "thresQ": thresQ, "qvect": qvect}
 
 
-def dose_filter(images, shapePadded, pixelsize, voltage, doseFiltParam, imageSum, normalize=False, dt=None):
-    """Unblur-style dose-weighted sum.  zorro.py:2349-2494."""
-    m = images.shape[0]
+def dose_filter_setup(m, shapePadded, pixelsize, voltage, doseFiltParam, imageSum, normalize=False, dt=None):
+    """The frame-independent part of doseFilter (zorro.py:2375-2452): the
+    constants, the q mesh and critical-dose map, the accumulators."""
     p = dose_filter_params(m, shapePadded, pixelsize, voltage, doseFiltParam, imageSum, dt)
     N, M = shapePadded
     xm, ym = np.meshgrid(np.arange(-M / 2, M / 2), np.arange(-N / 2, N / 2))
@@ -647,26 +647,46 @@ def dose_filter(images, shapePadded, pixelsize, voltage, doseFiltParam, imageSum
         qmesh = np.fft.fftshift(np.sqrt(xm * xm * (p["invPSx"] ** 2) + ym * ym * (p["invPSy"] ** 2)))
         crit = p["vs"] * (p["A"] * qmesh ** p["B"] + p["C"])
     crit[int(N / 2), int(M / 2)] = crit[int(N / 2), int(M / 2) - 1] ** 2
-    padW = np.array(shapePadded) - np.array(imageSum.shape)
-    acc = np.zeros(shapePadded, dtype=dt.c)
-    fmag = np.zeros(shapePadded, dtype=dt.f)
+    return {"p": p, "qmesh": qmesh, "crit": crit, "shapePadded": shapePadded, "out_shape": imageSum.shape,
+            "padW": np.array(shapePadded) - np.array(imageSum.shape), "acc": np.zeros(shapePadded, dtype=dt.c),
+            "fmag": np.zeros(shapePadded, dtype=dt.f), "normalize": normalize, "dt": dt}
+
+
+def dose_filter_add(st, frame, J):
+    """Frame J's filtered spectrum added to the accumulator (the loop body of
+    zorro.py:2455-2480)."""
+    p, dt = st["p"], st["dt"]
+    padW = st["padW"]
     with np.errstate(all="ignore"):
-        for J in range(m):
-            filt = np.exp(np.float32(-0.5 * p["accum"][J + 1]) / crit)
-            thres = np.exp(-(qmesh / p["thresQ"][J]) ** p["order"])
-            padded = np.pad(images[J].astype(dt.c), ((0, padW[0]), (0, padW[1])), mode="symmetric")
-            F = dt.fft2(padded)
-            if normalize:
-                cur = thres * filt
-                fmag += cur
-                acc += F * cur
-            else:
-                acc += F * thres * filt
-    if normalize:
-        out = dt.ifft2(acc * (np.float32(1.0) / (fmag + np.float32(1.0))))
+        filt = np.exp(np.float32(-0.5 * p["accum"][J + 1]) / st["crit"])
+        thres = np.exp(-(st["qmesh"] / p["thresQ"][J]) ** p["order"])
+        padded = np.pad(frame.astype(dt.c), ((0, padW[0]), (0, padW[1])), mode="symmetric")
+        F = dt.fft2(padded)
+        if st["normalize"]:
+            cur = thres * filt
+            st["fmag"] += cur
+            st["acc"] += F * cur
+        else:
+            st["acc"] += F * thres * filt
+
+
+def dose_filter_finish(st):
+    """The inverse transform, abs and crop of doseFilter (zorro.py:2482-2494)."""
+    dt = st["dt"]
+    if st["normalize"]:
+        out = dt.ifft2(st["acc"] * (np.float32(1.0) / (st["fmag"] + np.float32(1.0))))
     else:
-        out = dt.ifft2(acc)
-    return np.abs(out[:imageSum.shape[0], :imageSum.shape[1]])
+        out = dt.ifft2(st["acc"])
+    H, W = st["out_shape"]
+    return np.abs(out[:H, :W])
+
+
+def dose_filter(images, shapePadded, pixelsize, voltage, doseFiltParam, imageSum, normalize=False, dt=None):
+    """Unblur-style dose-weighted sum.  zorro.py:2349-2494."""
+    st = dose_filter_setup(images.shape[0], shapePadded, pixelsize, voltage, doseFiltParam, imageSum, normalize, dt)
+    for J in range(images.shape[0]):
+        dose_filter_add(st, images[J], J)
+    return dose_filter_finish(st)
 
 
 def psf_kernel(psf="K2", dt=None):
@@ -795,7 +815,20 @@ DEFAULTS = dict(shapeBinned=None, shapePadded=[4096, 4096], fouCrop=[3072, 3072]
                             "cutoffLower": -4.0, "cutoffUpper": 3.25, "neighborPix": 0})
 
 
-def even_odd_frc(aligned, o, fp64=True, workers=1):
+def half_set_sum(stack, o, translations, fp64=True, workers=1):
+    """The aligned sum of a half set for given drift translations: the
+    half-set registration's hot-pixel filter (when the settings have one) and
+    applyShifts (zorro.py:1734-1808) without the correlation and the solve."""
+    dt = Dtypes(fp64, workers)
+    images = np.array(stack, copy=True)
+    if "hot" in (o.get("filterMode") or "").lower():
+        images, _, _ = hotpix_filter(images, dict(o["hotpixInfo"]), dt=dt)
+    _, s = apply_shifts(images, translations, o["originMode"], o["shiftMethod"], o["subPixReg"],
+                        shapePadded=o["shapePadded"], dt=dt)
+    return s
+
+
+def even_odd_frc(aligned, o, fp64=True, workers=1, half_trans=None, capture=None):
     """Independent half-set FRC.  zorro.py:2099-2224 (xcorr='tri').
 
     The even and odd frames of the aligned stack are registered again by two
@@ -813,15 +846,28 @@ def even_odd_frc(aligned, o, fp64=True, workers=1):
     sub["doLazyFRC"] = False
     hot = "hot" in (o.get("filterMode") or "").lower()
     sub["filterMode"] = "hot" if hot else None
-    ev = align_image_stack(aligned[0::2], fp64=fp64, workers=workers, **dict(sub, hotpixInfo=dict(o["hotpixInfo"])))
-    od = align_image_stack(aligned[1::2], fp64=fp64, workers=workers, **dict(sub, hotpixInfo=dict(o["hotpixInfo"])))
+    if half_trans is None:
+        ev = align_image_stack(aligned[0::2], fp64=fp64, workers=workers,
+                               **dict(sub, hotpixInfo=dict(o["hotpixInfo"])))
+        od = align_image_stack(aligned[1::2], fp64=fp64, workers=workers,
+                               **dict(sub, hotpixInfo=dict(o["hotpixInfo"])))
+        te, to = ev["translations"], od["translations"]
+        se, so = ev["imageSum"], od["imageSum"]
+        if capture is not None:
+            capture["even"], capture["odd"] = ev["errorDict"], od["errorDict"]
+    else:
+        # the FRC that given half-set trajectories lead to (the half-set
+        # registrations' correlation and solve replaced by ``half_trans``)
+        te, to = (np.asarray(t) for t in half_trans)
+        se = half_set_sum(aligned[0::2], sub, te, fp64, workers)
+        so = half_set_sum(aligned[1::2], sub, to, fp64, workers)
     dt = Dtypes(fp64, workers)
-    pair = np.stack([ev["imageSum"], od["imageSum"]]).astype(dt.f)
+    pair = np.stack([se, so]).astype(dt.f)
     eo = align_image_stack(pair, fp64=fp64, workers=workers,
                            **dict(sub, triMode="first", hotpixInfo=dict(o["hotpixInfo"])))
-    trans = np.hstack([ev["translations"], od["translations"]])
+    trans = np.hstack([te, to])
     frc, frc2d, _ = tiled_frc(eo["images"][0], eo["images"][1], trans, dt=dt)
-    return frc, frc2d, ev["translations"], od["translations"]
+    return frc, frc2d, te, to
 
 
 def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
@@ -890,8 +936,10 @@ def align_image_stack(images, *, fp64=True, workers=1, capture=None, **attrs):
     bench["shifts1"] = time.time()
     res.update({"translations": t, "imageSum": imageSum, "errorDict": ed, "images": images})
     if o["doEvenOddFRC"]:
-        frc, frc2d, te, to = even_odd_frc(images, o, fp64=fp64, workers=workers)
-        res.update({"FRC": frc, "FRC2D": frc2d, "transEven": te, "transOdd": to})
+        halves = {}
+        frc, frc2d, te, to = even_odd_frc(images, o, fp64=fp64, workers=workers, capture=halves)
+        res.update({"FRC": frc, "FRC2D": frc2d, "transEven": te, "transOdd": to, "halfSetErrorDicts": halves,
+                    "settings": o})
     elif o["doLazyFRC"]:
         frc, frc2d, tiles = lazy_frc(images, t, dt=dt)
         res.update({"FRC": frc, "FRC2D": frc2d, "frc_tiles": tiles})

@@ -1,8 +1,8 @@
 """Generate the .zor fixtures by running the UNMODIFIED reference's
 saveConfig / loadConfig (zorro/zorro.py:3682-4075) through
-oracle/ref_harness.py.
+oracle/ref_harness.py (``ZORRO_REF_ROOT`` names the reference checkout).
 
-    python tests/golden/make_config_golden.py
+    ZORRO_REF_ROOT=<checkout> python tests/golden/make_config_golden.py
 
 Writes tests/golden/config_ref.zor (the reference's saveConfig of the state
 in ``config_state()``) and tests/golden/config_ref_loaded.json (what the

@@ -1,9 +1,9 @@
 """Generate the golden fixtures by running the UNMODIFIED reference.
 
-Run from the repository root where a checkout of LBEM-CH/zorro exists
-(default ``/root/reference``, override with ``ZORRO_REF_ROOT``):
+Run from the repository root with ``ZORRO_REF_ROOT`` naming a checkout of
+LBEM-CH/zorro (required; the directory that holds ``zorro/zorro.py``):
 
-    python tests/golden/make_golden.py
+    ZORRO_REF_ROOT=<checkout> python tests/golden/make_golden.py
 
 Each case regenerates its input movie from ``zorro_gb300.synthetic`` with a
 fixed seed, runs ``ImageRegistrator.alignImageStack`` through

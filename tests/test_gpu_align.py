@@ -190,40 +190,43 @@ def test_hot_pixels_and_gain():
     assert rel_l2(reg.imageSum, isum) <= SUM_TOL
 
 
-def test_golden_fixtures():
-    """Against the unmodified reference's own outputs (tests/golden)."""
+def _golden_names():
+    from tests.golden.make_golden import CASES as GC
+    return sorted(GC)
+
+
+@pytest.mark.parametrize("name", _golden_names())
+def test_golden_fixtures(name):
+    """Against the unmodified reference's own outputs (tests/golden), one
+    case per test so that a log names every case compared or skipped."""
     from tests.golden.make_golden import CASES as GC, input_checksum
-    skipped = []
-    for name, case in sorted(GC.items()):
-        g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")))
-        mv = make_movie(**case["movie"])
-        if input_checksum(mv["images"]) != str(g["checksum"]):
-            skipped.append(name)  # the synthetic input differs on this platform
-            continue
-        attrs = dict(case["attrs"])
-        if case["movie"].get("dtype") == "uint8":
-            reg = gpu_align(mv["raw"], gain=mv["gain"], **attrs)
-        else:
-            reg = gpu_align(mv["images"].copy(), **attrs)
-        tri = g["corrTriMat"] != 0
-        d = np.abs(reg.errorDictList[-1]["shiftsTriMat"] - g["shiftsTriMat"]).max(axis=2)[tri]
-        assert np.mean(d < 1e-9) >= 0.95, (name, d)
-        same_traj = np.abs(reg.translations - g["translations"]).max() <= TRAJ_TOL
-        vals = np.asarray(reg.imageSum, np.float64).reshape(-1)[g["imageSum_idx"]]
-        if same_traj:
-            assert np.linalg.norm(vals - g["imageSum_val"]) / np.linalg.norm(g["imageSum_val"]) <= SUM_TOL, name
-        if same_traj and "FRC" in g and not np.all(np.isnan(g["FRC"])):
-            assert np.nanmax(np.abs(reg.FRC - g["FRC"])) <= FRC_TOL, name
-        if "hot_guessHotpix" in g:
-            # exact against the oracle on this platform; the fixture was made on
-            # another NumPy/SciPy build, whose normal-CDF fit (L-BFGS-B) can
-            # move a pixel sitting on the cut-off
-            ref = zo.align_image_stack(mv["images"], **attrs)
-            for k in ("guessDeadpix", "guessHotpix", "neighborPix"):
-                assert reg.hotpixInfo[k] == ref["hotpixInfo"][k], (name, k)
-                assert abs(reg.hotpixInfo[k] - int(g["hot_" + k])) <= 1 + 0.01 * int(g["hot_" + k]), (name, k)
-    if len(skipped) == len(GC):
-        pytest.skip("synthetic inputs differ on this platform: %s" % skipped)
+    case = GC[name]
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")))
+    mv = make_movie(**case["movie"])
+    if input_checksum(mv["images"]) != str(g["checksum"]):
+        pytest.skip("%s: the synthetic input differs on this platform" % name)
+    attrs = dict(case["attrs"])
+    if case["movie"].get("dtype") == "uint8":
+        reg = gpu_align(mv["raw"], gain=mv["gain"], **attrs)
+    else:
+        reg = gpu_align(mv["images"].copy(), **attrs)
+    tri = g["corrTriMat"] != 0
+    d = np.abs(reg.errorDictList[-1]["shiftsTriMat"] - g["shiftsTriMat"]).max(axis=2)[tri]
+    assert np.mean(d < 1e-9) >= 0.95, (name, d)
+    same_traj = np.abs(reg.translations - g["translations"]).max() <= TRAJ_TOL
+    vals = np.asarray(reg.imageSum, np.float64).reshape(-1)[g["imageSum_idx"]]
+    if same_traj:
+        assert np.linalg.norm(vals - g["imageSum_val"]) / np.linalg.norm(g["imageSum_val"]) <= SUM_TOL, name
+    if same_traj and "FRC" in g and not np.all(np.isnan(g["FRC"])):
+        assert np.nanmax(np.abs(reg.FRC - g["FRC"])) <= FRC_TOL, name
+    if "hot_guessHotpix" in g:
+        # exact against the oracle on this platform; the fixture was made on
+        # another NumPy/SciPy build, whose normal-CDF fit (L-BFGS-B) can
+        # move a pixel sitting on the cut-off
+        ref = zo.align_image_stack(mv["images"], **attrs)
+        for k in ("guessDeadpix", "guessHotpix", "neighborPix"):
+            assert reg.hotpixInfo[k] == ref["hotpixInfo"][k], (name, k)
+            assert abs(reg.hotpixInfo[k] - int(g["hot_" + k])) <= 1 + 0.01 * int(g["hot_" + k]), (name, k)
 
 
 def test_even_odd_frc_against_oracle():

@@ -15,7 +15,7 @@ pytestmark = pytest.mark.gpu
 # (frames, frame shape, padded, crop, maxShift)
 CASES = [(6, (200, 180), (256, 256), (128, 128), 20),
          (5, (900, 1000), (1024, 1024), (1024, 1024), 100),
-         (12, (1500, 1400), (2048, 2048), (2048, 2048), 100)]  # 66 pairs: 8 waves of the scratch
+         (12, (1500, 1400), (2048, 2048), (2048, 2048), 100)]  # 66 pairs of 1,644,800 bytes: 7 waves of 10
 
 
 @pytest.mark.parametrize("n,shape,P,C_,mS", CASES)
@@ -58,8 +58,18 @@ def test_noalloc_rejects_bad_arguments():
     assert "null" in _lib.last_error()
     torch = gh.torch_mod()
     dummy = torch.zeros(16, dtype=torch.float32, device="cuda")
-    p = dummy.data_ptr()
-    rc = lib.zr_xcorr_pairs_noalloc(C.c_void_p(p), C.c_void_p(p), C.c_void_p(p), 1, 2, 8192, 8192, 20, C.c_void_p(p),
-                                    None)
+    p = C.c_void_p(dummy.data_ptr())
+    # a crop the kernels do not take: the same ZR_ESIZE as zr_xcorr_pairs
+    rc = lib.zr_xcorr_pairs_noalloc(p, p, p, 1, 2, 8192, 8192, 20, p, None)
     assert rc == -3
-    assert "8192" in _lib.last_error()
+    assert "crop" in _lib.last_error()
+    # maxShift below 2: ZR_ESIZE, as zr_xcorr_pairs returns
+    for ms in (0, 1):
+        rc = lib.zr_xcorr_pairs_noalloc(p, p, p, 1, 2, 128, 128, ms, p, None)
+        assert rc == -3, ms
+        assert "maxShift" in _lib.last_error()
+    # valid sizes whose one pair (1200 rows x 2052 columns x 8 bytes = 19.7 MB)
+    # does not fit the 16 MiB array
+    rc = lib.zr_xcorr_pairs_noalloc(p, p, p, 1, 2, 4096, 4096, 600, p, None)
+    assert rc == -3
+    assert "static scratch" in _lib.last_error()

@@ -46,8 +46,10 @@ extern "C" int zr_xcorr_pairs_noalloc(const void* G, const float* terms, const i
                                       int C1, int max_shift, float* cwin, void* stream) {
   if (!G || !terms || !pairs || !cwin || N <= 0) return set_error(ZR_EINVAL, "zr_xcorr_pairs_noalloc: null argument");
   if (M <= 0) return ZR_OK;
-  if (C1 <= 0 || max_shift <= 0) return set_error(ZR_EINVAL, "zr_xcorr_pairs_noalloc: bad crop or maxShift");
-  const size_t per_pair = (size_t)2 * max_shift * zr_spectrum_pitch(C1) * sizeof(float2);
+  // sizes outside the kernels' range (crop, maxShift < 2) get zr_xcorr_pairs'
+  // own ZR_ESIZE below; only a pair too large for the array is refused here
+  const size_t per_pair =
+      (C1 > 0 && max_shift > 0) ? (size_t)2 * max_shift * zr_spectrum_pitch(C1) * sizeof(float2) : 0;
   if (per_pair > (size_t)ZR_XCORR_STATIC_SCRATCH)
     return set_error(ZR_ESIZE,
                      "zr_xcorr_pairs_noalloc: one pair needs %zu bytes of scratch (crop %d, maxShift %d), more than "

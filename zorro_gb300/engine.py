@@ -229,7 +229,10 @@ class Engine:
         of hstack([transEven, transOdd]).  The half-set registrators do not
         recurse (the reference's own inherit doEvenOddFRC=True from the saved
         config and recurse until a half-set is too small to fit).  Returns
-        FRC (all rings), FRC2D, transEven, transOdd."""
+        FRC (all rings), FRC2D, transEven, transOdd and the half-set
+        registrations' error dictionaries ({'even': ..., 'odd': ...}; the
+        reference discards its half-set registrators, this keeps their pair
+        measurements for inspection)."""
         from .registrator import ImageRegistrator, copy_config
         torch = self.torch
         N, H, W = (int(v) for v in aligned.shape)
@@ -295,8 +298,9 @@ class Engine:
         nr = int(np.ceil(np.sqrt(2.0 * (box // 2) ** 2))) + 1
         if len(offs) and (offs.min() < 0 or (offs[:, 0] + box).max() > H or (offs[:, 1] + box).max() > W):
             raise ValueError("tiledFRC: tiles %s leave the %dx%d image (negative crop limits)" % (tiles, H, W))
+        halves = {"even": ev.errorDictList[-1], "odd": od.errorDictList[-1]}
         if len(offs) == 0:
-            return np.full(nr, np.nan), np.full((box, box), np.nan, dtype=np.float32), te, to
+            return np.full(nr, np.nan), np.full((box, box), np.nan, dtype=np.float32), te, to, halves
         pair = eo.images.contiguous()
         offs_dev = torch.from_numpy(offs.reshape(-1)).to(self.dev, non_blocking=True)
         fwb = self.lib.zr_frc_work_bytes(len(offs), box)
@@ -304,7 +308,7 @@ class Engine:
         fr = self.tensor("frc_eo", (nr,), torch.float64)
         self.call("H_frc", "zr_tiled_frc", pair[0].data_ptr(), pair[1].data_ptr(), H, W, box, offs_dev.data_ptr(),
                   len(offs), f2.data_ptr(), fr.data_ptr(), nr, self.ptr("frcwork", fwb), fwb, self.stream)
-        return fr, f2, te, to
+        return fr, f2, te, to, halves
 
     def _frames(self, raw, rtype, gain, ha=None, hb=None, gdiv=0.0):
         N, H, W = raw.shape
@@ -805,8 +809,8 @@ class Engine:
         # ---- lazy FRC (zorro.py:2226-2310)
         frc = frc2d = None
         if reg.doEvenOddFRC:
-            frc, frc2d, out["transEven"], out["transOdd"] = self._even_odd_frc(reg, aligned, hotinfo, filt,
-                                                                               aligned_ready)
+            frc, frc2d, out["transEven"], out["transOdd"], out["halfSetErrorDicts"] = self._even_odd_frc(
+                reg, aligned, hotinfo, filt, aligned_ready)
         elif reg.doLazyFRC:
             offs, tiles = hm.frc_tiles((H, W), translations)
             box = 512

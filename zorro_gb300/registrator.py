@@ -88,6 +88,9 @@ class ImageRegistrator:
         self.FRC2D = None
         self.transEven = None   # half-set trajectories of doEvenOddFRC
         self.transOdd = None
+        # addition: the half-set registrations' error dictionaries of
+        # doEvenOddFRC ({'even': ..., 'odd': ...}); the reference discards them
+        self.halfSetErrorDicts = None
         self.CTFProgram = None
         self.CTFInfo = {"DefocusU": None, "DefocusV": None, "DefocusAngle": None, "CtfFigureOfMerit": None,
                         "FinalResolution": None, "AmplitudeContrast": 0.07, "AdditionalPhaseShift": None}
