@@ -116,6 +116,54 @@ def test_fourier_binning_matches_oracle(shape, binned):
     assert err < 2e-5, err
 
 
+@pytest.mark.parametrize("shape,binned", [((8184, 11520), (4092, 5760)), ((11520, 8184), (5760, 4092))])
+def test_fourier_binning_superres(shape, binned):
+    """Four K3 super-resolution frames (11520 x 8184, either orientation)
+    binned 2x to 5760 x 4092 against the float64 oracle's binStack: the
+    11520-point side transformed directly by the mixed-radix engine (a
+    Bluestein convolution would need 32768 points), the 8184-point side and
+    the binned sides by Bluestein."""
+    import ctypes as C
+    import os
+    from tests import gpu_helpers as gh
+    from zorro_gb300 import _lib
+    torch = gh.torch_mod()
+    lib = _lib.load()
+    _lib.call("zr_init", torch.cuda.current_device())
+    mv = make_movie(4, shape, seed=41, mean_dose=0.25, drift_sigma=1.0)
+    raw = gh.dev_tensor(mv["images"].astype(np.float32))
+    fr = gh.frames_of(raw)
+    wb = lib.zr_bin_work_bytes(shape[0], shape[1], binned[0], binned[1])
+    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+    out = torch.zeros((4, binned[0], binned[1]), dtype=torch.float32, device="cuda")
+    _lib.call("zr_bin_fourier", C.byref(fr), binned[0], binned[1], out.data_ptr(), work.data_ptr(), wb, gh.stream())
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    del raw, work, out
+    ref = zo.bin_stack(mv["images"], binned, zo.Dtypes(True, os.cpu_count() or 1))
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    print("%s -> %s: max err %.2e of max, rel L2 %.2e" % (shape, binned, err, rel))
+    assert err < 2e-5 and rel < 1e-5, (err, rel)
+
+
+def test_fourier_binning_refuses_unsupported_long_sides():
+    """A side above 8192 that the engine cannot transform directly (and whose
+    Bluestein convolution does not fit one CTA) is refused with ZR_ESIZE."""
+    import ctypes as C
+    from tests import gpu_helpers as gh
+    from zorro_gb300 import _lib
+    torch = gh.torch_mod()
+    lib = _lib.load()
+    raw = torch.zeros((1, 600, 9000), dtype=torch.float32, device="cuda")
+    fr = gh.frames_of(raw)
+    dummy = torch.zeros(16, dtype=torch.float32, device="cuda")
+    rc = lib.zr_bin_fourier(C.byref(fr), 520, 4500, C.c_void_p(dummy.data_ptr()), C.c_void_p(dummy.data_ptr()),
+                            C.c_size_t(1 << 40), None)
+    assert rc == -3
+    assert "9216" in _lib.last_error()
+
+
 def _stream():
     import ctypes
     import torch

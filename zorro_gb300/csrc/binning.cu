@@ -4,12 +4,17 @@
 // normConst = 1/(Hb Wb), the unscaled Hb x Wb inverse DFT, and its real part.
 //
 // Frame sizes are arbitrary (K2 super-resolution frames are 7676 x 7420), so
-// every length-n DFT here is Bluestein's: with the chirp c_m = exp(i pi m^2/n),
+// a length-n DFT with n <= 8192 is Bluestein's: with the chirp
+// c_m = exp(i pi m^2/n),
 //     X_k = conj(c_k) sum_j (x_j conj(c_j)) c_{k-j},
 // a linear convolution done as a circular one of power-of-two length
 // M >= 2n - 1 with the shared-memory engine (forward FFT, product with the
-// transformed chirp, unscaled inverse, 1/M).  An inverse DFT is the conjugate
-// of the forward DFT of the conjugate.
+// transformed chirp, unscaled inverse, 1/M).  Longer sides (the 11520-pixel
+// width of K3 super-resolution frames) would need M = 32768, more than one
+// CTA's shared memory holds; they are transformed directly by the mixed-radix
+// engine when they divide its twiddle table (2^a 3^b 5^c, b <= 2, c <= 1:
+// 9216, 10240, 11520, 12288, 15360 and 16384).  An inverse DFT is the
+// conjugate of the forward DFT of the conjugate.
 //
 // Passes (one frame at a time, scratch in ``work``):
 //   rows     two real rows per complex Bluestein DFT of length W, split by
@@ -67,9 +72,17 @@ __global__ void __launch_bounds__(BN_T) k_bluestein_plan(int n, float2* __restri
 // Forward DFT of length n of the values already in sm[pidx(j)] (j < n; the
 // rest must be zero): X_k = conj(c_k) (IFFT(FFT(x conj(c)) bhat))_k / M, left
 // in sm[pidx(k)] for k < n.  All threads call; ends synchronised.
+//
+// With n == M (a length the engine transforms directly) it is the plain
+// forward FFT of the n values; ``c`` and ``bhat`` are not read.
 template <int M>
 __device__ void bluestein_inplace(float2* sm, int n, const float2* __restrict__ c, const float2* __restrict__ bhat,
                                   const float2* __restrict__ tw) {
+  if (n == M) {
+    __syncthreads();
+    block_fft<M, 1, BN_T, -1>(sm, tw);
+    return;
+  }
   for (int j = threadIdx.x; j < n; j += BN_T) sm[pidx(j)] = cmulc(sm[pidx(j)], __ldg(c + j));
   __syncthreads();
   block_fft<M, 1, BN_T, -1>(sm, tw);
@@ -206,9 +219,24 @@ static int bn_smem(const void* fn, size_t extra = 0) {
     case 2048: { constexpr int MM = 2048; __VA_ARGS__; } break;    \
     case 4096: { constexpr int MM = 4096; __VA_ARGS__; } break;    \
     case 8192: { constexpr int MM = 8192; __VA_ARGS__; } break;    \
+    case 9216: { constexpr int MM = 9216; __VA_ARGS__; } break;    \
+    case 10240: { constexpr int MM = 10240; __VA_ARGS__; } break;  \
+    case 11520: { constexpr int MM = 11520; __VA_ARGS__; } break;  \
+    case 12288: { constexpr int MM = 12288; __VA_ARGS__; } break;  \
+    case 15360: { constexpr int MM = 15360; __VA_ARGS__; } break;  \
     case 16384: { constexpr int MM = 16384; __VA_ARGS__; } break;  \
     default: return set_error(ZR_ESIZE, "binning transform of %d points not supported", (int)(M)); \
   }
+
+// Transform length for a side of n pixels: the Bluestein convolution length
+// (n <= 8192), n itself when the engine transforms it directly, else 0.
+static int bn_len(int n) {
+  if (n >= 2 && n <= 8192) return bn_pow2_at_least(2 * n - 1) < 2048 ? 2048 : bn_pow2_at_least(2 * n - 1);
+  if (n > 8192 && n <= 16384 && TWN % n == 0 && (n == 9216 || n == 10240 || n == 11520 || n == 12288 ||
+                                                  n == 15360 || n == 16384))
+    return n;
+  return 0;
+}
 
 struct BnPlan {
   int n, M;
@@ -219,6 +247,7 @@ static size_t bn_plan_bytes(int n) { return ((size_t)n + bn_pow2_at_least(2 * n 
 
 template <int M>
 static int bn_make_plan(BnPlan& p, const float2* tw, cudaStream_t st) {
+  if (p.n == M) return ZR_OK;  // a direct transform: no chirp
   ZR_TRY(bn_smem<M>((const void*)k_bluestein_plan<M>));
   k_bluestein_plan<M><<<1, BN_T, ld_of(M) * sizeof(float2), st>>>(p.n, p.c, p.bhat, tw);
   return launched("k_bluestein_plan");
@@ -243,11 +272,11 @@ extern "C" int zr_bin_fourier(const zr_frames_t* frames, int Hb, int Wb, float* 
   if (Hb < 2 || Wb < 2 || (Hb & 1) || (Wb & 1) || Hb > H || Wb > W)
     return set_error(ZR_ESIZE, "zr_bin_fourier: binned shape %dx%d must be even and no larger than %dx%d", Hb, Wb,
                      H, W);
-  const int MW = bn_pow2_at_least(2 * W - 1), MH = bn_pow2_at_least(2 * H - 1);
-  const int MHb = bn_pow2_at_least(2 * Hb - 1), MWb = bn_pow2_at_least(2 * Wb - 1);
-  if (MW > 16384 || MH > 16384 || MHb < 2048 || MWb < 2048)
-    return set_error(ZR_ESIZE, "zr_bin_fourier: frame %dx%d -> %dx%d: every side must be in 513..8192", H, W, Hb,
-                     Wb);
+  const int MW = bn_len(W), MH = bn_len(H), MHb = bn_len(Hb), MWb = bn_len(Wb);
+  if (!MW || !MH || !MHb || !MWb || Hb < 513 || Wb < 513)
+    return set_error(ZR_ESIZE,
+                     "zr_bin_fourier: frame %dx%d -> %dx%d: every side must be in 513..8192, or one of 9216, 10240, "
+                     "11520, 12288, 15360, 16384 (binned sides at least 513)", H, W, Hb, Wb);
   if (work_bytes < zr_bin_work_bytes(H, W, Hb, Wb))
     return set_error(ZR_EWORK, "zr_bin_fourier: work buffer %zu < %zu", work_bytes, zr_bin_work_bytes(H, W, Hb, Wb));
   const float2* tw = twiddles();
@@ -293,6 +322,9 @@ extern "C" int zr_bin_fourier(const zr_frames_t* frames, int Hb, int Wb, float* 
     ZR_BN_COLS(16384, 16384) ZR_BN_COLS(16384, 8192) ZR_BN_COLS(16384, 4096) ZR_BN_COLS(16384, 2048)
     ZR_BN_COLS(8192, 8192) ZR_BN_COLS(8192, 4096) ZR_BN_COLS(8192, 2048)
     ZR_BN_COLS(4096, 4096) ZR_BN_COLS(4096, 2048) ZR_BN_COLS(2048, 2048)
+    ZR_BN_COLS(9216, 16384) ZR_BN_COLS(9216, 8192) ZR_BN_COLS(10240, 16384) ZR_BN_COLS(10240, 8192)
+    ZR_BN_COLS(11520, 16384) ZR_BN_COLS(11520, 8192) ZR_BN_COLS(12288, 16384) ZR_BN_COLS(12288, 8192)
+    ZR_BN_COLS(15360, 16384) ZR_BN_COLS(15360, 8192)
     return set_error(ZR_ESIZE, "zr_bin_fourier: column lengths %d -> %d not supported", H, Hb);
 #undef ZR_BN_COLS
     k_bin_transpose<<<dim3((Hb + 31) / 32, (Kb + 31) / 32), dim3(32, 8), 0, st>>>(Ci, Kb, Hb, Ri);

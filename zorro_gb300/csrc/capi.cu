@@ -37,7 +37,7 @@ int launched(const char* what) {
   return cuda_check(cudaGetLastError(), what);
 }
 
-// W_8192^k = exp(-2 pi i k / 8192), one copy per device.
+// W_TWN^k = exp(-2 pi i k / TWN), one copy per device.
 static __device__ float2 d_twiddle[TWN];
 
 static std::mutex g_init_mu;

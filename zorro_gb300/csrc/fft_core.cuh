@@ -1,7 +1,7 @@
 // Batched complex FFTs held in shared memory, for sm_103a.
 //
 // A CTA transforms NB sequences of length L (L = 2^a 3^b 5^c dividing TWN,
-// e.g. 64..16384 and 3 x 2^k) that sit in shared memory.  Element i of sequence b lives at s[b*ld(L) + pidx(i)]:
+// e.g. 64..16384, 3 x 2^k and 9 x 2^k) that sit in shared memory.  Element i of sequence b lives at s[b*ld(L) + pidx(i)]:
 // one padding slot every 16 elements keeps the radix-16 scatter of the first
 // pass free of bank conflicts, and the row pitch (ld_of) keeps tiles of 4
 // sequences x 4 elements conflict-free.  Each pass is a radix-16 Stockham
@@ -12,7 +12,7 @@
 // passes.
 //
 // Twiddles come from a table of W_TWN^k = exp(-2 pi i k / TWN), TWN = 2^14 x
-// 3 x 5, computed in double precision on the host and rounded to float
+// 3^2 x 5, computed in double precision on the host and rounded to float
 // (``tw`` argument); a length-L transform reads every (TWN/L)-th entry.
 // DIR = -1 is the forward transform, +1 the inverse; neither is normalised.
 #pragma once
@@ -21,7 +21,7 @@
 
 namespace zr {
 
-constexpr int TWN = 245760;  // twiddle table length: 2^14 * 3 * 5
+constexpr int TWN = 737280;  // twiddle table length: 2^14 * 3^2 * 5
 
 __host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 4); }
 // Row pitch of one sequence: the padded length rounded so that pitch = 4
@@ -258,7 +258,7 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
 // memory.  Saves one store and one load of every element in shared memory.
 template <int L, int NB, int T, int DIR, typename Load>
 __device__ __forceinline__ void block_fft_from(float2* s, const float2* __restrict__ tw, Load load) {
-  static_assert(L >= 2 && TWN % L == 0, "L must divide the twiddle table length 2^14 * 3 * 5");
+  static_assert(L >= 2 && TWN % L == 0, "L must divide the twiddle table length 2^14 * 3^2 * 5");
   constexpr int R = fft_radix(L);
   constexpr int LR = L / R;
   constexpr int NBF = NB * LR;
@@ -293,7 +293,7 @@ __device__ __forceinline__ void block_fft_from(float2* s, const float2* __restri
 // before (after filling ``s``); the function ends with a barrier.
 template <int L, int NB, int T, int DIR>
 __device__ __forceinline__ void block_fft(float2* s, const float2* __restrict__ tw) {
-  static_assert(L >= 2 && TWN % L == 0, "L must divide the twiddle table length 2^14 * 3 * 5");
+  static_assert(L >= 2 && TWN % L == 0, "L must divide the twiddle table length 2^14 * 3^2 * 5");
   fft_pass<L, NB, T, DIR, 1>(s, tw);
 }
 

@@ -25,8 +25,9 @@
 
 namespace zr {
 
-constexpr int PK_T = 512;
-constexpr int PK_RB = 8;       // rows per vertical-filter block
+constexpr int PK_T = 1024;
+constexpr int PK_NW = PK_T / 32;  // warps
+constexpr int PK_RB = 16;      // rows per vertical-filter block
 constexpr int PK_MAXR = 64;    // largest filter radius
 constexpr int PK_SUBR = 8;     // +/- patch half-size (zorro.py:619)
 
@@ -34,11 +35,18 @@ struct PkShared {
   double gw[2 * PK_MAXR + 1];
   float wy[2 * PK_MAXR + 1];
   float wx[2 * PK_MAXR + 1];
-  double red[PK_T / 32][3];
-  float redf[PK_T / 32];
-  int redi[PK_T / 32];
+  double red[PK_NW][3];
+  float redf[PK_NW];
+  int redi[PK_NW];
+  float ws1[PK_NW], ws2[PK_NW], wmx[PK_NW];  // per-warp partials of the filter statistics
+  int wcnt[PK_NW];
   double bc[4];
   int bi[2];
+  double st_s1, st_s2;  // block totals of the filter statistics
+  float st_mx;
+  int st_n;
+  double x;             // the Brent search's next abscissa (thread 0 -> all)
+  int go;               // 1 while the search continues
 };
 
 __device__ __forceinline__ int reflect_idx(int i, int n) {
@@ -88,9 +96,9 @@ __device__ double3 block_sum3(PkShared& sh, double a, double b, double c) {
   if (lane == 0) { sh.red[wid][0] = a; sh.red[wid][1] = b; sh.red[wid][2] = c; }
   __syncthreads();
   if (wid == 0) {
-    a = lane < PK_T / 32 ? sh.red[lane][0] : 0.0;
-    b = lane < PK_T / 32 ? sh.red[lane][1] : 0.0;
-    c = lane < PK_T / 32 ? sh.red[lane][2] : 0.0;
+    a = lane < PK_NW ? sh.red[lane][0] : 0.0;
+    b = lane < PK_NW ? sh.red[lane][1] : 0.0;
+    c = lane < PK_NW ? sh.red[lane][2] : 0.0;
     for (int o = 16; o > 0; o >>= 1) {
       a += __shfl_down_sync(0xffffffffu, a, o);
       b += __shfl_down_sync(0xffffffffu, b, o);
@@ -115,8 +123,8 @@ __device__ void block_argmax(PkShared& sh, float& v, int& idx) {
   if (lane == 0) { sh.redf[wid] = v; sh.redi[wid] = idx; }
   __syncthreads();
   if (wid == 0) {
-    v = lane < PK_T / 32 ? sh.redf[lane] : -INFINITY;
-    idx = lane < PK_T / 32 ? sh.redi[lane] : 0x7fffffff;
+    v = lane < PK_NW ? sh.redf[lane] : -INFINITY;
+    idx = lane < PK_NW ? sh.redi[lane] : 0x7fffffff;
     for (int o = 16; o > 0; o >>= 1) {
       const float ov = __shfl_down_sync(0xffffffffu, v, o);
       const int oi = __shfl_down_sync(0xffffffffu, idx, o);
@@ -135,6 +143,42 @@ struct FiltStats {
   float mx;        // max f
   int n;
 };
+
+// Block totals of the per-thread filter statistics: float sums within each
+// warp (a shuffle tree), the warps' partials summed in double by warp 0 in a
+// fixed order; the count exactly, the maximum.  All threads must call; every
+// thread receives the totals.  (The float64 pipe only sees one warp's worth
+// of additions.)
+__device__ void block_stats(PkShared& sh, float s1, float s2, int cnt, float mx, FiltStats& st) {
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  }
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) { sh.ws1[wid] = s1; sh.ws2[wid] = s2; sh.wcnt[wid] = cnt; sh.wmx[wid] = mx; }
+  __syncthreads();
+  if (wid == 0) {
+    double a = lane < PK_NW ? (double)sh.ws1[lane] : 0.0;
+    double b = lane < PK_NW ? (double)sh.ws2[lane] : 0.0;
+    int n = lane < PK_NW ? sh.wcnt[lane] : 0;
+    float m = lane < PK_NW ? sh.wmx[lane] : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+      n += __shfl_down_sync(0xffffffffu, n, o);
+      m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    }
+    if (lane == 0) { sh.st_s1 = a; sh.st_s2 = b; sh.st_n = n; sh.st_mx = m; }
+  }
+  __syncthreads();
+  st.s1 = sh.st_s1;
+  st.s2 = sh.st_s2;
+  st.n = sh.st_n;
+  st.mx = sh.st_mx;
+  __syncthreads();  // the totals are read before any later call writes them
+}
 
 constexpr int PK_TX = 64;            // column lanes of the filter passes
 constexpr int PK_TY = PK_T / PK_TX;  // rows per block (== PK_RB)
@@ -202,14 +246,7 @@ __device__ void filter_pass(const float* C, float* V, const int* rtab, int w, in
     }
     __syncthreads();
   }
-  double3 r = block_sum3(sh, (double)s1, (double)s2, (double)cnt);
-  st.s1 = r.x;
-  st.s2 = r.y;
-  st.n = (int)r.z;
-  float m = mx;
-  int dummy = 0;
-  block_argmax(sh, m, dummy);
-  st.mx = m;
+  block_stats(sh, s1, s2, cnt, mx, st);
   if (MODE == 1) {
     block_argmax(sh, bv, bi);
     amax = bv;
@@ -221,9 +258,9 @@ __device__ void filter_pass(const float* C, float* V, const int* rtab, int w, in
 // filters 4 consecutive columns; the vertical taps are float4 loads, the
 // horizontal taps slide a 4-wide register window one column at a time.
 // Rows per thread of the vectorised filter pass (register blocking of the
-// vertical pass): 4 while the window, the row block and the static shared
-// memory fit in one SM's shared memory, else 2.
-__host__ __device__ constexpr int pk_vec_rows(int w) { return w <= 216 ? 4 : 2; }
+// vertical pass): 2, which keeps a thread within the 64 registers of a
+// 1024-thread CTA.
+__host__ __device__ constexpr int pk_vec_rows(int) { return 2; }
 __host__ __device__ constexpr int pk_vec_pitch(int w) { return w + 8; }
 
 // Horizontal pass of one row for 4 consecutive outputs x0..x0+3 away from
@@ -354,14 +391,7 @@ __device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, i
     }
     __syncthreads();
   }
-  double3 r = block_sum3(sh, (double)s1, (double)s2, (double)cnt);
-  st.s1 = r.x;
-  st.s2 = r.y;
-  st.n = (int)r.z;
-  float m = mx;
-  int dummy = 0;
-  block_argmax(sh, m, dummy);
-  st.mx = m;
+  block_stats(sh, s1, s2, cnt, mx, st);
   if (MODE == 1) {
     block_argmax(sh, bv, bi);
     amax = bv;
@@ -373,15 +403,15 @@ template <int MODE>
 __device__ void filter_any(const float* C, float* V, const int* rtab, int w, int mS, int ry, int rx, const float* wy,
                            const float* wx, float c, PkShared& sh, bool use_mask, FiltStats& st, float& amax,
                            int& aidx) {
-  if ((w & 3) == 0 && w >= 16 && w <= 4 * PK_TX) {
-    if (pk_vec_rows(w) == 4)
-      filter_pass4<MODE, 4>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
-    else
-      filter_pass4<MODE, 2>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
-  } else
+  if ((w & 3) == 0 && w >= 16 && w <= 4 * PK_TX)
+    filter_pass4<MODE, pk_vec_rows(0)>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
+  else
     filter_pass<MODE>(C, V, rtab, w, mS, ry, rx, wy, wx, c, sh, use_mask, st, amax, aidx);
 }
 
+// std(G_sigma * C) / (max - mean) of the filtered window (zorro.py:1108-
+// 1121).  All threads filter; the value is formed by thread 0 only (the
+// others return 0).
 __device__ double objective(const float* C, float* V, const int* rtab, int w, int mS, double sigma, float c,
                             PkShared& sh) {
   const int r = gauss_weights(sigma, sh.wy, sh);
@@ -390,6 +420,7 @@ __device__ double objective(const float* C, float* V, const int* rtab, int w, in
   float am;
   int ai;
   filter_any<0>(C, V, rtab, w, mS, r, r, sh.wy, sh.wy, c, sh, false, st, am, ai);
+  if (threadIdx.x != 0) return 0.0;
   const double n = (double)st.n;
   const double m1 = st.s1 / n;
   const double var = st.s2 / n - m1 * m1;
@@ -400,9 +431,13 @@ __device__ double objective(const float* C, float* V, const int* rtab, int w, in
 __device__ __forceinline__ double sgn1(double v) { return v > 0.0 ? 1.0 : (v < 0.0 ? -1.0 : 1.0); }
 
 // Bounded Brent minimisation (FMM FMIN).  Returns the abscissa of the best
-// value; *nfev receives the number of function values.
+// value (to every thread); *nfev receives the number of function values.
+// The search's scalar state lives in thread 0, which decides each next
+// abscissa and whether to go on and hands them to the CTA through shared
+// memory; all threads evaluate the objective.
 __device__ double fmin_bounded(const float* C, float* V, const int* rtab, int w, int mS, float c, PkShared& sh,
                                double lo, double hi, double xatol, int maxfun, int* nfev) {
+  const bool lead = threadIdx.x == 0;
   const double sqrt_eps = sqrt(2.2e-16);
   const double golden = 0.5 * (3.0 - sqrt(5.0));
   double a = lo, b = hi;
@@ -416,7 +451,12 @@ __device__ double fmin_bounded(const float* C, float* V, const int* rtab, int w,
   double xm = 0.5 * (a + b);
   double tol1 = sqrt_eps * fabs(xf) + xatol / 3.0;
   double tol2 = 2.0 * tol1;
-  while (fabs(xf - xm) > (tol2 - 0.5 * (b - a))) {
+  // thread 0: the next abscissa of the loop below, or the end of the search
+  auto next_point = [&]() {
+    if (!(fabs(xf - xm) > (tol2 - 0.5 * (b - a)))) {
+      sh.go = 0;
+      return;
+    }
     bool gstep = true;
     if (fabs(e) > tol1) {
       gstep = false;
@@ -441,43 +481,51 @@ __device__ double fmin_bounded(const float* C, float* V, const int* rtab, int w,
       rat = golden * e;
     }
     x = xf + sgn1(rat) * fmax(fabs(rat), tol1);
-    const double fu = objective(C, V, rtab, w, mS, x, c, sh);
-    num += 1;
-    if (fu <= fx) {
-      if (x >= xf) a = xf; else b = xf;
-      fulc = nfc; ffulc = fnfc;
-      nfc = xf; fnfc = fx;
-      xf = x; fx = fu;
-    } else {
-      if (x < xf) a = x; else b = x;
-      if ((fu <= fnfc) || (nfc == xf)) {
+    sh.x = x;
+    sh.go = 1;
+  };
+  if (lead) next_point();
+  __syncthreads();
+  while (sh.go) {
+    const double xe = sh.x;
+    const double fu = objective(C, V, rtab, w, mS, xe, c, sh);  // barriers: every thread has read sh.x, sh.go
+    if (lead) {
+      num += 1;
+      if (fu <= fx) {
+        if (x >= xf) a = xf; else b = xf;
         fulc = nfc; ffulc = fnfc;
-        nfc = x; fnfc = fu;
-      } else if ((fu <= ffulc) || (fulc == xf) || (fulc == nfc)) {
-        fulc = x; ffulc = fu;
+        nfc = xf; fnfc = fx;
+        xf = x; fx = fu;
+      } else {
+        if (x < xf) a = x; else b = x;
+        if ((fu <= fnfc) || (nfc == xf)) {
+          fulc = nfc; ffulc = fnfc;
+          nfc = x; fnfc = fu;
+        } else if ((fu <= ffulc) || (fulc == xf) || (fulc == nfc)) {
+          fulc = x; ffulc = fu;
+        }
+      }
+      xm = 0.5 * (a + b);
+      tol1 = sqrt_eps * fabs(xf) + xatol / 3.0;
+      tol2 = 2.0 * tol1;
+      if (num >= maxfun) sh.go = 0;
+      else next_point();
+      if (!sh.go) {
+        sh.x = xf;
+        sh.bi[1] = num;
       }
     }
-    xm = 0.5 * (a + b);
-    tol1 = sqrt_eps * fabs(xf) + xatol / 3.0;
-    tol2 = 2.0 * tol1;
-    if (num >= maxfun) break;
+    __syncthreads();
   }
-  *nfev = num;
-  return xf;
-}
-
-// Filtered value of the window at (y, x) (used for the 16 x 16 patch).
-__device__ float filtered_at(const float* C, int w, int y, int x, int ry, int rx, const float* wy, const float* wx) {
-  float f = 0.0f;
-  for (int kx = -rx; kx <= rx; kx++) {
-    const int xx = reflect_idx(x + kx, w);
-    float acc = 0.0f;
-    if (ry == 0) acc = C[y * w + xx];
-    else
-      for (int ky = -ry; ky <= ry; ky++) acc = fmaf(wy[ky + ry], C[reflect_idx(y + ky, w) * w + xx], acc);
-    f = (rx == 0) ? acc : fmaf(wx[kx + rx], acc, f);
+  if (lead && num == 1) {  // the search ended before its first step
+    sh.x = xf;
+    sh.bi[1] = num;
   }
-  return f;
+  __syncthreads();
+  const double best = sh.x;
+  *nfev = sh.bi[1];
+  __syncthreads();
+  return best;
 }
 
 // The sub-pixel step on a 16 x 16 filtered patch (zorro.py:1180-1216): its
@@ -575,10 +623,12 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
     __syncthreads();
   }
   // mean of the window: the centring constant of the one-pass variances
+  // (any value near the mean serves; the statistics are exact sums around it)
   float ls = 0.0f;
   for (int e = threadIdx.x; e < w2; e += PK_T) ls += C[e];
-  double3 tot = block_sum3(sh, (double)ls, 0.0, 0.0);
-  const float c = (float)(tot.x / (double)w2);
+  FiltStats tot;
+  block_stats(sh, ls, 0.0f, 0, 0.0f, tot);
+  const float c = (float)(tot.s1 / (double)w2);
 
   double sigy = 0.0, sigx = 0.0, sig_opt = nan("");
   int nfev = 0;
@@ -597,42 +647,62 @@ __global__ void __launch_bounds__(PK_T, 1) k_peaks(const float* __restrict__ cwi
   int aidx = 0;
   filter_any<1>(C, V, rtab, w, mS, ry, rx, sh.wy, sh.wx, c, sh, p.use_mask != 0, st, amax, aidx);
   const int cy = aidx / w, cx = aidx - (aidx / w) * w;
-  double peaksig = nan("");
-  {
-    const double n = (double)st.n;
-    const double m1 = st.s1 / n;
-    const double var = st.s2 / n - m1 * m1;
-    const double mean = (double)c + m1;
-    peaksig = ((double)amax - mean) / sqrt(var > 0.0 ? var : 0.0);
-  }
   const float cval = C[cy * w + cx];
-  double shy = (double)cy - w / 2.0, shx = (double)cx - w / 2.0;
   float corr = cval;
   int flags = 0;
+  int sy = -1, sx = -1;  // sub-pixel argmax on the upsampled grid
+  float bv = 0.0f;
   const int sp = p.sub_pix_reg;
+  const int L = 16 * sp;
   if (sp > 1) {
     if (cy - PK_SUBR >= 0 && cy + PK_SUBR <= w && cx - PK_SUBR >= 0 && cx + PK_SUBR <= w) {
-      // 16 x 16 filtered patch, then its forward DFT
+      // the 16 x 16 filtered patch around the peak, separably: the vertical
+      // pass for its 16 rows over the 16 + 2 rx columns the horizontal taps
+      // reach (reflected), then the horizontal pass; the same multiply-adds
+      // in the same order as the full filter pass, so the same values
       __shared__ float patch[16 * 16];
-      for (int e = threadIdx.x; e < 256; e += PK_T) {
-        const int i = e >> 4, j = e & 15;
-        patch[e] = filtered_at(C, w, cy - PK_SUBR + i, cx - PK_SUBR + j, ry, rx, sh.wy, sh.wx);
+      const int pw = 16 + 2 * rx;
+      for (int e = threadIdx.x; e < 16 * pw; e += PK_T) {
+        const int i = e / pw, j = e - (e / pw) * pw;
+        const int y = cy - PK_SUBR + i;
+        const int xx = reflect_idx(cx - PK_SUBR - rx + j, w);
+        float acc = 0.0f;
+        if (ry == 0) acc = C[y * w + xx];
+        else
+          for (int k = 0; k <= 2 * ry; k++) acc = fmaf(sh.wy[k], C[rtab[PK_MAXR + y - ry + k] * w + xx], acc);
+        V[e] = acc;
       }
       __syncthreads();
-      const int L = 16 * sp;
-      float bv;
+      for (int e = threadIdx.x; e < 256; e += PK_T) {
+        const int i = e >> 4, j = e & 15;
+        float f = 0.0f;
+        if (rx == 0) f = V[i * pw + j];
+        else
+          for (int k = 0; k <= 2 * rx; k++) f = fmaf(sh.wx[k], V[i * pw + j + k], f);
+        patch[e] = f;
+      }
+      __syncthreads();
       int bi;
       subpix_search(patch, sp, tw, (float2*)C, patchF, sh, bv, bi);  // the window is no longer needed
-      const int sy = bi / L, sx = bi - (bi / L) * L;
-      const double ry0 = (double)cy - w / 2.0, rx0 = (double)cx - w / 2.0;
-      shy = ry0 + ((double)sy - L / 2.0 + (ry0 > 0 ? 1.0 : (ry0 < 0 ? -1.0 : 0.0))) / sp;
-      shx = rx0 + ((double)sx - L / 2.0 + (rx0 > 0 ? 1.0 : (rx0 < 0 ? -1.0 : 0.0))) / sp;
-      corr = (float)((double)bv / 256.0);
+      sy = bi / L;
+      sx = bi - (bi / L) * L;
     } else {
       flags |= 1;
     }
   }
   if (threadIdx.x == 0) {
+    const double n = (double)st.n;
+    const double m1 = st.s1 / n;
+    const double var = st.s2 / n - m1 * m1;
+    const double mean = (double)c + m1;
+    const double peaksig = ((double)amax - mean) / sqrt(var > 0.0 ? var : 0.0);
+    double shy = (double)cy - w / 2.0, shx = (double)cx - w / 2.0;
+    if (sy >= 0) {
+      const double ry0 = (double)cy - w / 2.0, rx0 = (double)cx - w / 2.0;
+      shy = ry0 + ((double)sy - L / 2.0 + (ry0 > 0 ? 1.0 : (ry0 < 0 ? -1.0 : 0.0))) / sp;
+      shx = rx0 + ((double)sx - L / 2.0 + (rx0 > 0 ? 1.0 : (rx0 < 0 ? -1.0 : 0.0))) / sp;
+      corr = (float)((double)bv / 256.0);
+    }
     zr_peak_result_t r;
     r.shift_y = shy;
     r.shift_x = shx;
@@ -981,7 +1051,10 @@ extern "C" int zr_locate_peaks(const float* cwin, int M, int max_shift, const zr
   // w + 8 for the vectorised layout, PK_RB rows otherwise)
   const bool vec = (w & 3) == 0 && w >= 16 && w <= 4 * PK_TX;
   const size_t vrows = vec ? (size_t)(PK_T / (w / 4)) * pk_vec_rows(w) : (size_t)PK_RB;
-  const size_t vbuf = vrows * (vec ? pk_vec_pitch(w) : w) * sizeof(float);
+  size_t vbuf = vrows * (vec ? pk_vec_pitch(w) : w) * sizeof(float);
+  // the row block also holds the vertical pass of the 16 x 16 sub-pixel patch
+  const size_t pbuf = (size_t)16 * (16 + 2 * PK_MAXR) * sizeof(float);
+  if (vbuf < pbuf) vbuf = pbuf;
   size_t smem = (size_t)w * w * sizeof(float) + vbuf;
   const size_t sub = (size_t)17 * 16 * params->sub_pix_reg * sizeof(float2);
   if (params->sub_pix_reg > 1 && (size_t)w * w * sizeof(float) < sub) smem = sub + vbuf;
