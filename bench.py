@@ -501,6 +501,133 @@ def run_reference(args, wl, rank, world):
 
 # ----------------------------------------------------------------------------- GPU arm
 
+def mixed_sources(torch, dev):
+    """The three detector shapes of the batched and served workloads
+    (zorro_gb300.workloads.CONFIG4), one seeded 60-frame movie each on the
+    device; a movie of n frames is the first n frames of its shape's."""
+    from zorro_gb300.workloads import config4_movies
+    out = {}
+    for name, (mv, attrs, count) in config4_movies(n_frames=60).items():
+        raw = torch.from_numpy(mv["raw"]).to(dev)
+        gain = torch.from_numpy(mv["gain"]).to(dev) if mv["gain"] is not None else None
+        out[name] = (raw, gain, attrs, count, str(mv["raw"].dtype))
+    return out
+
+
+def _mixed_reg(raw, gain, attrs, dev):
+    from zorro_gb300.registrator import ImageRegistrator
+    r = ImageRegistrator()
+    for k, v in attrs.items():
+        setattr(r, k, v)
+    r.images = raw
+    r.gainRef = gain
+    r.keepAlignedImages = False
+    r.returnDeviceArrays = True
+    r.device = dev.index or 0
+    return r
+
+
+def batch_leg(args, torch, dev, lib, dist, world, barrier, sources):
+    """The batched uneven workload (CONFIG4): 16 movies, 8 K2 (40 frames),
+    5 float16 4096^2 (30 frames), 3 super-resolution (50 frames), each slot
+    its own device copy of its shape's movie (the copies' work is real,
+    their results equal).  Movies/s of alignImageStacks over the 16 against
+    the same 16 through alignImageStack one at a time, and the kernel
+    launches of each."""
+    from zorro_gb300.registrator import alignImageStacks
+    from zorro_gb300.workloads import CONFIG4
+    slots = []
+    for name, (raw, gain, attrs, count, _) in sources.items():
+        n = CONFIG4[name]["movie"]["n_frames"]
+        for _ in range(count):
+            slots.append((raw[:n].clone(), gain, attrs, name))
+
+    def regs():
+        return [_mixed_reg(raw, gain, attrs, dev) for raw, gain, attrs, _ in slots]
+    alignImageStacks(regs())
+    barrier()
+    nb = max(1, min(args.steps, 3))
+    l0 = lib.zr_launch_count()
+    b0 = torch.cuda.Event(enable_timing=True)
+    b1 = torch.cuda.Event(enable_timing=True)
+    b0.record()
+    for _ in range(nb):
+        alignImageStacks(regs())
+    b1.record()
+    barrier()
+    t_batch = slowest_rank(b0.elapsed_time(b1) / 1000.0 / nb, dist, dev)
+    launches_batch = (lib.zr_launch_count() - l0) // nb
+    # the same movies one at a time (after one warm-up movie of each shape)
+    seen = set()
+    for r, (_, _, _, name) in zip(regs(), slots):
+        if name not in seen:
+            seen.add(name)
+            r.alignImageStack()
+    barrier()
+    l0 = lib.zr_launch_count()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record()
+    for r in regs():
+        r.alignImageStack()
+    p1.record()
+    barrier()
+    t_plain = slowest_rank(p0.elapsed_time(p1) / 1000.0, dist, dev)
+    launches_plain = lib.zr_launch_count() - l0
+    n = len(slots)
+    del slots
+    return {"value": round(world * n / t_batch, 3), "unit": UNIT, "movies": n,
+            "mix": {k: v[3] for k, v in sources.items()},
+            "frames": {k: CONFIG4[k]["movie"]["n_frames"] for k in sources},
+            "shapes": {k: "%dx%d %s" % (v[0].shape[1], v[0].shape[2], v[4]) for k, v in sources.items()},
+            "ms_per_batch": round(t_batch * 1e3, 2), "plain_value": round(world * n / t_plain, 3),
+            "vs_plain": round(t_plain / t_batch, 3), "launches_per_batch": int(launches_batch),
+            "launches_plain": int(launches_plain)}
+
+
+def served_mix_leg(args, torch, dev, sources, rank):
+    """The served workload (CONFIG5): at each arrival rate, Poisson arrivals
+    for ``--poisson-seconds`` seconds, each request a movie of a shape drawn
+    50/30/20 with its frame count uniform in [20, 60], admitted by free
+    device memory under the 160 GB budget into the server's slots; latency is
+    arrival to result.  Per rate: requests, movies/s, p50 and p99."""
+    from zorro_gb300.serve import MovieServer
+    from zorro_gb300.workloads import CONFIG5
+    rng = np.random.default_rng(11 + rank)
+    names = list(CONFIG5["mix"])
+    probs = np.array([CONFIG5["mix"][k] for k in names])
+    lo, hi = CONFIG5["frames"]
+    srv = MovieServer(device=dev.index or 0, slots=args.slots, hbm_budget=CONFIG5["hbm_budget"])
+    # warm-up: one movie of each shape at the largest frame count
+    for name in names:
+        raw, gain, attrs, _, _ = sources[name]
+        srv.submit(_mixed_reg(raw[:hi], gain, attrs, dev)).result()
+    out = []
+    for rate in CONFIG5["rates"]:
+        srv.reset_stats()
+        n_req = max(4, int(round(args.poisson_seconds * rate)))
+        gaps = rng.exponential(1.0 / rate, size=n_req)
+        picks = rng.choice(len(names), size=n_req, p=probs)
+        frames = rng.integers(lo, hi + 1, size=n_req)
+        t_next = time.perf_counter()
+        futs = []
+        for g, k, n in zip(gaps, picks, frames):
+            t_next += g
+            while time.perf_counter() < t_next:
+                time.sleep(min(0.002, max(0.0, t_next - time.perf_counter())))
+            raw, gain, attrs, _, _ = sources[names[k]]
+            futs.append(srv.submit(_mixed_reg(raw[:int(n)], gain, attrs, dev)))
+        for f in futs:
+            f.result()
+        st_ = srv.stats()
+        out.append({"rate_per_s": rate, "requests": n_req,
+                    "shapes": {nm: int(np.sum(picks == i)) for i, nm in enumerate(names)},
+                    "movies_per_s": round(st_["movies_per_s"], 3), "p50_ms": round(st_["p50_s"] * 1e3, 2),
+                    "p99_ms": round(st_["p99_s"] * 1e3, 2)})
+    srv.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -512,9 +639,10 @@ def main():
     ap.add_argument("--slots", type=int, default=2, help="movies in flight on the served path")
     ap.add_argument("--profile-only", action="store_true", help="run the warm-up and 2 steps, no timing output")
     ap.add_argument("--no-poisson", action="store_true", help="skip the open-loop Poisson-arrival serving runs")
-    ap.add_argument("--poisson-seconds", type=float, default=3.0, help="arrival window per Poisson rate")
+    ap.add_argument("--poisson-seconds", type=float, default=6.0, help="arrival window per Poisson rate")
     ap.add_argument("--no-fp16", action="store_true", help="skip the half-precision-spectra run")
     ap.add_argument("--no-packed4", action="store_true", help="skip the 4-bit (MRC mode 101) end-to-end run")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven 16-movie run")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -636,26 +764,6 @@ def main():
     barrier()
     t_served = (time.perf_counter() - sv0) / (args.steps * args.slots)
     served = srv.stats()
-    # open-loop serving: Poisson arrivals at fixed rates, latency = arrival to result
-    poisson = []
-    if not args.no_poisson:
-        rng = np.random.default_rng(7 + rank)
-        for rate in (2.0, 8.0, 32.0):
-            srv.reset_stats()
-            n_req = max(8, int(args.poisson_seconds * rate))
-            gaps = rng.exponential(1.0 / rate, size=n_req)
-            t_start = time.perf_counter()
-            futs = []
-            for g in gaps:
-                t_start += g
-                while time.perf_counter() < t_start:
-                    time.sleep(min(0.002, max(0.0, t_start - time.perf_counter())))
-                futs.append(srv.submit(make_reg(raw_dev, gain_dev, True)))
-            for f in futs:
-                f.result()
-            st_ = srv.stats()
-            poisson.append({"rate_per_s": rate, "requests": n_req, "movies_per_s": round(st_["movies_per_s"], 3),
-                            "p50_ms": round(st_["p50_s"] * 1e3, 2), "p99_ms": round(st_["p99_s"] * 1e3, 2)})
     srv.close()
     t_served = slowest_rank(t_served, dist, dev)
 
@@ -727,6 +835,18 @@ def main():
                    "unpack_ms": round(t_unpack * 1e3, 4), "unpack_gbs": round(ub / t_unpack / 1e9, 1),
                    "unpack_frac": round(ub / t_unpack / 1e9 / peak_, 3)}
 
+    # ---- batched uneven launch: 16 movies of three detector shapes (8 K2,
+    # 5 float16 4096^2, 3 super-resolution binned 2x) registered as one batch,
+    # against the same 16 movies registered one at a time
+    batched = served_mix = None
+    if not (args.no_batch and args.no_poisson):
+        sources = mixed_sources(torch, dev)
+        if not args.no_batch:
+            batched = batch_leg(args, torch, dev, lib, dist, world, barrier, sources)
+        if not args.no_poisson:
+            served_mix = served_mix_leg(args, torch, dev, sources, rank)
+        del sources
+
     # ---- roofline of the dominant stage
     w = 2 * wl["attrs"]["maxShift"]
     C = int(wl["attrs"]["fouCrop"][0])
@@ -776,9 +896,11 @@ def main():
                         "d2h_bytes_per_step": d2h},
                 "served": {"value": round(world / t_served, 3), "unit": UNIT, "slots": args.slots,
                            "p50_ms": round(served["p50_s"] * 1e3, 2), "p99_ms": round(served["p99_s"] * 1e3, 2),
-                           "vs_plain": round((world / t_served) / value, 3), "poisson": poisson},
+                           "vs_plain": round((world / t_served) / value, 3)},
+                "served_mix": served_mix,
                 "fp16_spectra": fp16,
                 "e2e_packed4": packed4,
+                "batched": batched,
                 "gpu_launches": int(launches),
                 "wall_s_timed": round(wall, 3),
                 "clocks": clk.summary(),

@@ -56,6 +56,13 @@ typedef struct zr_frames {
   float gain_divisor;  /* 0: none */
   int n_frames, height, width;
   long long frame_stride; /* elements between frames, 0 = height*width */
+  /* Frames of several movies in one call (the batched path): frame n reads
+   * the maps of movie frame_movie[n] (device array of n_frames ints), which
+   * start map_stride elements apart in gain, hot_a and hot_b.  NULL: every
+   * frame reads the one [H][W] map set.  zr_gain_sum and zr_shift_sum work on
+   * one movie at a time and refuse it. */
+  const int* frame_movie;
+  long long map_stride;
 } zr_frames_t;
 
 /* Hot-pixel filter constants (zorro.py:2595-2649). */
@@ -346,6 +353,47 @@ size_t zr_dose_work_bytes(int P0, int P1, int n_frames);
 int zr_dose_filter(const float* aligned, int N, int H, int W, const zr_dose_params_t* params,
                    const float* thres_q, const float* dose_end, int P0, int P1, float* filt_sum,
                    void* work, size_t work_bytes, void* stream);
+
+/* ---- compressed movie files: MRCZ (zorro.loadData, zorro.py:3414) ---- */
+
+/* Decode one LZ4 block (blosc's LZ4 and LZ4HC codecs) of src_bytes into
+ * dst (dst_bytes available).  Host memory, host code.  Returns the decoded
+ * byte count, or -1 for a malformed block (nothing outside the buffers is
+ * read or written). */
+long long zr_lz4_decompress(const void* src, size_t src_bytes, void* dst, size_t dst_bytes);
+
+/* ---- planning: FFTW_MEASURE and wisdom, pyFFTWPlanner zorro_util.py:966-1066 ---- */
+
+/* A registration shape to plan for: padded size P0 x P1, Fourier crop
+ * C0 x C1, maxShift, and the number of synthetic frames to measure on
+ * (2..64; 8 is plenty). */
+typedef struct zr_plan_shape {
+  int P0, P1, C0, C1, max_shift, n_frames;
+} zr_plan_shape_t;
+
+/* Sequences per CTA (1, 2 or 4; 0 = the built-in default) of the forward
+ * row pass (for transforms of P1 points), the forward column pass (P0), the
+ * correlation column pass (C0) and the correlation row pass (C1), and the
+ * measured milliseconds of every candidate: ms_spectra[rows][cols] and
+ * ms_pairs[cols][rows] for the variants 1, 2, 4 in that order. */
+typedef struct zr_plan_choice {
+  int fwd_rows, fwd_cols, xc_cols, xc_rows;
+  float ms_spectra[3][3];
+  float ms_pairs[3][3];
+} zr_plan_choice_t;
+
+/* zr_plan measures, on the current device and ``stream``, the forward
+ * spectra of n_frames synthetic P0 x P1 frames and the correlation windows
+ * of all their pairs for every variant, keeps the fastest for this device
+ * (for every later call with those transform lengths) and reports the
+ * choice.  Blocking (it waits for its timings).  The variants split the
+ * same transforms differently between CTAs: results do not depend on the
+ * plan.  zr_plan_set installs a choice saved earlier (the caller's wisdom),
+ * zr_plan_get reads the installed one (0 = default). */
+size_t zr_plan_work_bytes(const zr_plan_shape_t* shape);
+int zr_plan(const zr_plan_shape_t* shape, void* work, size_t work_bytes, void* stream, zr_plan_choice_t* out);
+int zr_plan_set(const zr_plan_shape_t* shape, const zr_plan_choice_t* choice);
+int zr_plan_get(const zr_plan_shape_t* shape, zr_plan_choice_t* choice);
 
 #ifdef __cplusplus
 }

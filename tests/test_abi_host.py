@@ -1,6 +1,7 @@
 """CPU-only checks: the C ABI library loads and exports every symbol the
 header declares, and the host-side float64 steps of the product agree with
 the oracle.  No kernel is launched here."""
+import ctypes
 import os
 import re
 
@@ -290,3 +291,38 @@ def test_gain_reference_orientation(info):
     r = ImageRegistrator()
     r.gainInfo = dict(info)
     assert np.array_equal(r.loadGainRef(g), want)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every struct of include/zorro_gb300.h has the size and field offsets
+    of its ctypes mirror (a C program built against the header prints them)."""
+    import shutil
+    import subprocess
+    from zorro_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = {"zr_frames_t": _lib.Frames, "zr_hotpix_params_t": _lib.HotpixParams, "zr_peak_params_t": _lib.PeakParams,
+             "zr_peak_result_t": _lib.PeakResult, "zr_shift_t": _lib.Shift, "zr_dose_params_t": _lib.DoseParams,
+             "zr_plan_shape_t": _lib.PlanShape, "zr_plan_choice_t": _lib.PlanChoice}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "zorro_gb300.h"', "int main(void) {"]
+    for cname, cls in pairs.items():
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in cls._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        p = ln.split()
+        if len(p) == 3:
+            got[(p[0], p[1])] = int(p[2])
+    for cname, cls in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)

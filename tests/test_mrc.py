@@ -122,7 +122,7 @@ def test_bad_files(tmp_path):
     with pytest.raises(ValueError, match="header"):
         mrc.read(str(tmp_path / "tiny.mrc"))
     with pytest.raises(ValueError, match="compressed"):
-        mrc.read(str(tmp_path / "t.mrcz"))
+        mrc.read(str(tmp_path / "t.mrc.gz"))
     bad = bytearray(raw)
     struct.pack_into("<i", bad, 12, 3)  # mode 3 (complex int16) is not a movie mode
     (tmp_path / "m3.mrc").write_bytes(bytes(bad))
@@ -161,7 +161,7 @@ def test_load_data_raw_movie_and_gain(tmp_path):
         mo.write(str(tmp_path / "img.mrc"), raw[:1], 0)
         ImageRegistrator().loadData(str(tmp_path / "img.mrc"))
     with pytest.raises(ValueError, match="not supported"):
-        ImageRegistrator().loadData(str(tmp_path / "movie.dm4"))
+        ImageRegistrator().loadData(str(tmp_path / "movie.tif"))
 
 
 def test_save_data_names_and_contents(tmp_path, monkeypatch):

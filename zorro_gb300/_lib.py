@@ -23,13 +23,17 @@ EXPORTS = (
     "zr_l1_solve", "zr_xcorr_pairs_noalloc", "zr_logistic_fit", "zr_refine_spectra", "zr_refine_terms",
     "zr_xcorr_refine", "zr_pack_half", "zr_xcorr_terms_half", "zr_xcorr_pairs_half", "zr_bin_work_bytes",
     "zr_bin_fourier", "zr_unpack_u4", "zr_full_prepare", "zr_full_work_bytes", "zr_full_filter", "zr_full_peaks",
+    "zr_plan_work_bytes", "zr_plan", "zr_plan_set", "zr_plan_get", "zr_lz4_decompress",
 )
 
 
 class Frames(C.Structure):
+    """zr_frames_t.  ``frame_movie``/``map_stride`` (the batched path) stay
+    zero unless frames of several movies share a call."""
     _fields_ = [("raw", C.c_void_p), ("raw_type", C.c_int), ("gain", C.c_void_p), ("hot_a", C.c_void_p),
                 ("hot_b", C.c_void_p), ("gain_divisor", C.c_float), ("n_frames", C.c_int), ("height", C.c_int),
-                ("width", C.c_int), ("frame_stride", C.c_longlong)]
+                ("width", C.c_int), ("frame_stride", C.c_longlong), ("frame_movie", C.c_void_p),
+                ("map_stride", C.c_longlong)]
 
 
 class HotpixParams(C.Structure):
@@ -48,6 +52,16 @@ class PeakResult(C.Structure):
     _fields_ = [("shift_y", C.c_double), ("shift_x", C.c_double), ("sigma", C.c_double), ("corr", C.c_float),
                 ("peaksig", C.c_float), ("origin", C.c_float), ("cy", C.c_int), ("cx", C.c_int),
                 ("flags", C.c_int), ("nfev", C.c_int)]
+
+
+class PlanShape(C.Structure):
+    _fields_ = [("P0", C.c_int), ("P1", C.c_int), ("C0", C.c_int), ("C1", C.c_int), ("max_shift", C.c_int),
+                ("n_frames", C.c_int)]
+
+
+class PlanChoice(C.Structure):
+    _fields_ = [("fwd_rows", C.c_int), ("fwd_cols", C.c_int), ("xc_cols", C.c_int), ("xc_rows", C.c_int),
+                ("ms_spectra", (C.c_float * 3) * 3), ("ms_pairs", (C.c_float * 3) * 3)]
 
 
 class Shift(C.Structure):
@@ -117,6 +131,11 @@ _SIGS = {
     "zr_l1_solve": (C.c_int, [_P, _P, _P, C.c_int, C.c_int, C.c_double, C.c_double, _P, C.POINTER(C.c_int)]),
     "zr_dose_filter": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.POINTER(DoseParams), _P, _P, C.c_int, C.c_int,
                                  _P, _P, C.c_size_t, _P]),
+    "zr_plan_work_bytes": (C.c_size_t, [C.POINTER(PlanShape)]),
+    "zr_plan": (C.c_int, [C.POINTER(PlanShape), _P, C.c_size_t, _P, C.POINTER(PlanChoice)]),
+    "zr_plan_set": (C.c_int, [C.POINTER(PlanShape), C.POINTER(PlanChoice)]),
+    "zr_plan_get": (C.c_int, [C.POINTER(PlanShape), C.POINTER(PlanChoice)]),
+    "zr_lz4_decompress": (C.c_longlong, [_P, C.c_size_t, _P, C.c_size_t]),
 }
 
 

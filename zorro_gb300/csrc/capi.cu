@@ -66,6 +66,37 @@ static int init_device(int dev) {
   return ZR_OK;
 }
 
+// The planner's choices: per device, stage and transform length (a slot per
+// supported length), the chosen sequences per CTA (0: the default).
+static const int k_tune_lengths[] = {64, 128, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096, 6144};
+constexpr int k_tune_nlen = sizeof(k_tune_lengths) / sizeof(k_tune_lengths[0]);
+static int g_tune[64][TUNE_STAGES][k_tune_nlen];
+
+static int tune_slot(int length) {
+  for (int i = 0; i < k_tune_nlen; i++)
+    if (k_tune_lengths[i] == length) return i;
+  return -1;
+}
+
+int tune_get(int stage, int length) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || stage < 0 || stage >= TUNE_STAGES) return 0;
+  const int k = tune_slot(length);
+  return k < 0 ? 0 : g_tune[dev][stage][k];
+}
+
+int tune_set(int stage, int length, int value) {
+  int dev = 0;
+  ZR_TRY(cuda_check(cudaGetDevice(&dev), "cudaGetDevice"));
+  if (dev < 0 || dev >= 64 || stage < 0 || stage >= TUNE_STAGES) return set_error(ZR_EINVAL, "tune_set: bad stage");
+  const int k = tune_slot(length);
+  if (k < 0) return set_error(ZR_ESIZE, "tune_set: transform length %d has no variants", length);
+  if (value != 0 && value != 1 && value != 2 && value != 4)
+    return set_error(ZR_EINVAL, "tune_set: %d sequences per CTA (1, 2 or 4; 0 for the default)", value);
+  g_tune[dev][stage][k] = value;
+  return ZR_OK;
+}
+
 const float2* twiddles() {
   int dev = 0;
   if (cuda_check(cudaGetDevice(&dev), "cudaGetDevice") != ZR_OK) return nullptr;

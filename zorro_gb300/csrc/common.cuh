@@ -24,6 +24,8 @@ struct FrameSrc {
   float gdiv;
   int N, H, W;
   long long fstride;  // elements between consecutive frames
+  const int* fmap;    // frame -> movie whose maps it reads (null: one map set)
+  long long mstride;  // elements between the maps of consecutive movies
 };
 
 __host__ inline FrameSrc make_src(const zr_frames_t* f) {
@@ -38,7 +40,15 @@ __host__ inline FrameSrc make_src(const zr_frames_t* f) {
   s.H = f->height;
   s.W = f->width;
   s.fstride = f->frame_stride ? f->frame_stride : (long long)f->height * f->width;
+  s.fmap = f->frame_movie;
+  s.mstride = f->frame_movie ? f->map_stride : 0;
   return s;
+}
+
+// Offset of frame n's gain and hot-pixel maps (the batched path's frames
+// read the maps of their own movie).
+__device__ __forceinline__ long long map_off(const FrameSrc& f, int n) {
+  return f.fmap ? (long long)__ldg(f.fmap + n) * f.mstride : 0;
 }
 
 __device__ __forceinline__ float load_raw(const FrameSrc& f, long long idx) {
@@ -51,8 +61,9 @@ __device__ __forceinline__ float load_raw(const FrameSrc& f, long long idx) {
 }
 
 __device__ __forceinline__ float load_corrected(const FrameSrc& f, int n, int y, int x) {
-  const long long p = (long long)y * f.W + x;
-  float v = load_raw(f, (long long)n * f.fstride + p);
+  const long long q = (long long)y * f.W + x;
+  float v = load_raw(f, (long long)n * f.fstride + q);
+  const long long p = q + map_off(f, n);
   if (f.gain) v = __fmul_rn(__ldg(f.gain + p), v);
   if (f.gdiv != 0.0f) v = __fdiv_rn(v, f.gdiv);
   if (f.ha) v = __fmaf_rn(__ldg(f.ha + p), v, __ldg(f.hb + p));
@@ -64,6 +75,7 @@ __device__ __forceinline__ float load_corrected(const FrameSrc& f, int n, int y,
 // vector loads of every array).
 __device__ __forceinline__ float4 load4_corrected(const FrameSrc& f, int n, long long p) {
   const long long i = (long long)n * f.fstride + p;
+  const long long pm = p + map_off(f, n);
   float4 v;
   switch (f.type) {
     case ZR_U8: {
@@ -85,13 +97,13 @@ __device__ __forceinline__ float4 load4_corrected(const FrameSrc& f, int n, long
     default: v = __ldg(reinterpret_cast<const float4*>((const float*)f.raw + i));
   }
   if (f.gain) {
-    const float4 g = __ldg(reinterpret_cast<const float4*>(f.gain + p));
+    const float4 g = __ldg(reinterpret_cast<const float4*>(f.gain + pm));
     v = make_float4(__fmul_rn(g.x, v.x), __fmul_rn(g.y, v.y), __fmul_rn(g.z, v.z), __fmul_rn(g.w, v.w));
   }
   if (f.gdiv != 0.0f)
     v = make_float4(__fdiv_rn(v.x, f.gdiv), __fdiv_rn(v.y, f.gdiv), __fdiv_rn(v.z, f.gdiv), __fdiv_rn(v.w, f.gdiv));
   if (f.ha) {
-    const float4 a = __ldg(reinterpret_cast<const float4*>(f.ha + p)), b = __ldg(reinterpret_cast<const float4*>(f.hb + p));
+    const float4 a = __ldg(reinterpret_cast<const float4*>(f.ha + pm)), b = __ldg(reinterpret_cast<const float4*>(f.hb + pm));
     v = make_float4(__fmaf_rn(a.x, v.x, b.x), __fmaf_rn(a.y, v.y, b.y), __fmaf_rn(a.z, v.z, b.z),
                     __fmaf_rn(a.w, v.w, b.w));
   }
@@ -152,10 +164,11 @@ __device__ __forceinline__ void fetch4(const FrameSrc& f, int n, long long p, Px
     }
     default: q.raw = __ldg(reinterpret_cast<const uint4*>((const float*)f.raw + i));
   }
-  if (f.gain) q.g = __ldg(reinterpret_cast<const float4*>(f.gain + p));
+  const long long pm = p + map_off(f, n);
+  if (f.gain) q.g = __ldg(reinterpret_cast<const float4*>(f.gain + pm));
   if (f.ha) {
-    q.a = __ldg(reinterpret_cast<const float4*>(f.ha + p));
-    q.b = __ldg(reinterpret_cast<const float4*>(f.hb + p));
+    q.a = __ldg(reinterpret_cast<const float4*>(f.ha + pm));
+    q.b = __ldg(reinterpret_cast<const float4*>(f.hb + pm));
   }
 }
 

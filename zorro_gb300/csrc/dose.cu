@@ -24,6 +24,9 @@ namespace zr {
 #define ZR_DS_NBR 4
 #endif
 constexpr int DS_NBR = ZR_DS_NBR;
+// rows (columns) per CTA for a transform of length L: two for the 6144-point
+// transforms, whose four-row tiles would not fit the register file
+__host__ __device__ constexpr int ds_nbr(int L) { return L > 4096 ? 2 : DS_NBR; }
 // CTAs per SM to ask the register allocator for: 128 registers a thread
 constexpr int ds_minb(int T) { return T >= 512 ? 1 : 512 / T; }
 
@@ -34,10 +37,10 @@ __device__ __forceinline__ int sym_idx(int i, int n) {
 }
 
 template <int P1>
-__global__ void __launch_bounds__(fft_threads(P1, DS_NBR), ds_minb(fft_threads(P1, DS_NBR)))
+__global__ void __launch_bounds__(fft_threads(P1, ds_nbr(P1)), ds_minb(fft_threads(P1, ds_nbr(P1))))
     k_dose_rows(const float* __restrict__ img, int N, int H, int W, int f0, int K4, int P0,
                 float2* __restrict__ RW, const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(P1, DS_NBR);
+  constexpr int T = fft_threads(P1, ds_nbr(P1));
   constexpr int LD = ld_of(P1);
   extern __shared__ float2 sm[];
   const int g = blockIdx.x;
@@ -46,8 +49,8 @@ __global__ void __launch_bounds__(fft_threads(P1, DS_NBR), ds_minb(fft_threads(P
   const float* ia = img + (size_t)na * H * W;
   const float* ib = img + (size_t)(nb < N ? nb : na) * H * W;
   // element x of row r: the symmetric padding of the two frames' row
-  block_fft_from<P1, DS_NBR, T, -1>(sm, tw, [&](int r, int x) {
-    const int yy = g * DS_NBR + r;
+  block_fft_from<P1, ds_nbr(P1), T, -1>(sm, tw, [&](int r, int x) {
+    const int yy = g * ds_nbr(P1) + r;
     const int ys = yy < H ? yy : (yy < 2 * H ? 2 * H - 1 - yy : sym_idx(yy, H));
     const int xs = x < W ? x : (x < 2 * W ? 2 * W - 1 - x : sym_idx(x, W));
     const size_t p = (size_t)ys * W + xs;
@@ -56,9 +59,9 @@ __global__ void __launch_bounds__(fft_threads(P1, DS_NBR), ds_minb(fft_threads(P
   // output: column-major per frame, [frame][kx][ky]
   const size_t fa = (size_t)(2 * pl) * K4 * P0;
   const size_t fb = fa + (size_t)K4 * P0;
-  for (int e = threadIdx.x; e < K4 * DS_NBR; e += T) {
-    const int k = e / DS_NBR, r = e - k * DS_NBR;
-    const size_t o = (size_t)k * P0 + g * DS_NBR + r;
+  for (int e = threadIdx.x; e < K4 * ds_nbr(P1); e += T) {
+    const int k = e / ds_nbr(P1), r = e - k * ds_nbr(P1);
+    const size_t o = (size_t)k * P0 + g * ds_nbr(P1) + r;
     float2 U = make_float2(0.0f, 0.0f), V = U;
     if (k <= P1 / 2) {
       const float2 zk = sm[r * LD + pidx(k)];
@@ -162,14 +165,14 @@ __global__ void __launch_bounds__(DS_CT, 2)
 
 // Inverse column pass, keeping rows [0, H).
 template <int P0>
-__global__ void __launch_bounds__(fft_threads(P0, DS_NBR), ds_minb(fft_threads(P0, DS_NBR)))
+__global__ void __launch_bounds__(fft_threads(P0, ds_nbr(P0)), ds_minb(fft_threads(P0, ds_nbr(P0))))
     k_dose_icols(const float2* __restrict__ ACC, const float* __restrict__ FM, int normalize, int K4, int H,
                  float2* __restrict__ T2, const float2* __restrict__ tw) {
-  constexpr int T = fft_threads(P0, DS_NBR);
+  constexpr int T = fft_threads(P0, ds_nbr(P0));
   constexpr int LD = ld_of(P0);
   extern __shared__ float2 sm[];
-  const int k0 = blockIdx.x * DS_NBR;
-  block_fft_from<P0, DS_NBR, T, 1>(sm, tw, [&](int c, int y) {
+  const int k0 = blockIdx.x * ds_nbr(P0);
+  block_fft_from<P0, ds_nbr(P0), T, 1>(sm, tw, [&](int c, int y) {
     float2 v = __ldg(ACC + (size_t)(k0 + c) * P0 + y);
     if (normalize) {
       const float s = 1.0f / (__ldg(FM + (size_t)(k0 + c) * P0 + y) + 1.0f);
@@ -177,8 +180,8 @@ __global__ void __launch_bounds__(fft_threads(P0, DS_NBR), ds_minb(fft_threads(P
     }
     return v;
   });
-  for (int e = threadIdx.x; e < H * DS_NBR; e += T) {
-    const int y = e / DS_NBR, c = e - y * DS_NBR;
+  for (int e = threadIdx.x; e < H * ds_nbr(P0); e += T) {
+    const int y = e / ds_nbr(P0), c = e - y * ds_nbr(P0);
     T2[(size_t)y * K4 + k0 + c] = sm[c * LD + pidx(y)];
   }
 }
@@ -219,15 +222,17 @@ static int set_smem(const void* fn, size_t smem) {
     case 2048: { constexpr int LL = 2048; CALL; } break;        \
     case 3072: { constexpr int LL = 3072; CALL; } break;        \
     case 4096: { constexpr int LL = 4096; CALL; } break;        \
+    case 6144: { constexpr int LL = 6144; CALL; } break;        \
     default: return set_error(ZR_ESIZE, "dose filter size %d not supported", (int)(L)); \
   }
 
 template <int P1>
 static int dose_rows(const float* img, int N, int H, int W, int f0, int npairs, int K4, int P0, float2* RW,
                      const float2* tw, cudaStream_t st) {
-  const size_t smem = (size_t)DS_NBR * ld_of(P1) * sizeof(float2);
+  const size_t smem = (size_t)ds_nbr(P1) * ld_of(P1) * sizeof(float2);
   ZR_TRY(set_smem<P1>((const void*)k_dose_rows<P1>, smem));
-  k_dose_rows<P1><<<dim3(P0 / DS_NBR, npairs), fft_threads(P1, DS_NBR), smem, st>>>(img, N, H, W, f0, K4, P0, RW, tw);
+  k_dose_rows<P1><<<dim3(P0 / ds_nbr(P1), npairs), fft_threads(P1, ds_nbr(P1)), smem, st>>>(img, N, H, W, f0, K4, P0,
+                                                                                            RW, tw);
   return launched("k_dose_rows");
 }
 
@@ -244,9 +249,9 @@ static int dose_cols(const float2* RW, int f0, int nfr, int K4, int P1, const zr
 template <int P0>
 static int dose_icols(const float2* ACC, const float* FM, int normalize, int K4, int H, float2* T2, const float2* tw,
                       cudaStream_t st) {
-  const size_t smem = (size_t)DS_NBR * ld_of(P0) * sizeof(float2);
+  const size_t smem = (size_t)ds_nbr(P0) * ld_of(P0) * sizeof(float2);
   ZR_TRY(set_smem<P0>((const void*)k_dose_icols<P0>, smem));
-  k_dose_icols<P0><<<K4 / DS_NBR, fft_threads(P0, DS_NBR), smem, st>>>(ACC, FM, normalize, K4, H, T2, tw);
+  k_dose_icols<P0><<<K4 / ds_nbr(P0), fft_threads(P0, ds_nbr(P0)), smem, st>>>(ACC, FM, normalize, K4, H, T2, tw);
   return launched("k_dose_icols");
 }
 
@@ -280,9 +285,11 @@ extern "C" int zr_dose_filter(const float* aligned, int N, int H, int W, const z
   if (!aligned || !params || !thres_q || !dose_end || !filt_sum || !work)
     return set_error(ZR_EINVAL, "zr_dose_filter: null argument");
   if (N <= 0 || H <= 0 || W <= 0 || H > P0 || W > P1) return set_error(ZR_EINVAL, "zr_dose_filter: bad sizes");
-  if (!fft_len_ok(P0) || !fft_len_ok(P1) || P0 < 256 || P1 < 256 || P0 > 4096 || P1 > 4096)
-    return set_error(ZR_ESIZE, "zr_dose_filter: padded size %dx%d must be a power of two in [256, 4096], 1536 or 3072",
-                     P0, P1);
+  if (!fft_len_ok(P0) || !fft_len_ok(P1) || P0 < 256 || P1 < 256 || P0 > 6144 || P1 > 6144 || P0 == 8192 ||
+      P1 == 8192)
+    return set_error(ZR_ESIZE,
+                     "zr_dose_filter: padded size %dx%d must be a power of two in [256, 4096], 1536, 3072 or 6144", P0,
+                     P1);
   const size_t fixed = dose_fixed_bytes(P0, P1), per = dose_frame_bytes(P0, P1);
   if (work_bytes < fixed + 2 * per)
     return set_error(ZR_EWORK, "zr_dose_filter: work buffer %zu < %zu", work_bytes, fixed + 2 * per);

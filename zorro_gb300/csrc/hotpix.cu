@@ -308,6 +308,8 @@ static uint64_t first_false(P pred) {
 using namespace zr;
 
 extern "C" int zr_gain_sum(const zr_frames_t* frames, float* unaligned_sum, double* total, void* stream) {
+  if (frames && frames->frame_movie)
+    return set_error(ZR_EINVAL, "zr_gain_sum: one movie at a time (frame_movie must be NULL)");
   if (!frames || !frames->raw || !unaligned_sum) return set_error(ZR_EINVAL, "zr_gain_sum: null argument");
   FrameSrc f = make_src(frames);
   f.ha = nullptr;

@@ -15,8 +15,11 @@ const float2* twiddles();
 
 inline bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
 // Transform lengths the library is built for: powers of two and 3 x 2^k
-// (the reference's default Fourier crop is 3072).
-inline bool fft_len_ok(long long v) { return is_pow2(v) || v == 384 || v == 768 || v == 1536 || v == 3072; }
+// (the reference's default Fourier crop is 3072; 6144 pads the 5760-pixel
+// side of binned K3 super-resolution frames).
+inline bool fft_len_ok(long long v) {
+  return is_pow2(v) || v == 384 || v == 768 || v == 1536 || v == 3072 || v == 6144;
+}
 inline int ilog2(long long v) {
   int l = 0;
   while ((1LL << l) < v) ++l;
@@ -36,6 +39,16 @@ constexpr int fft_threads(int L, int NB, int ept = ZR_FFT_EPT) {
 }
 // Resident CTAs per SM to ask the register allocator for (short transforms).
 constexpr int fft_minblocks(int L) { return L <= 2048 ? ZR_FFT_MINB : 1; }
+
+// Launch variants of the transform kernels, chosen per transform length by
+// the planner (zr_plan) or set from saved choices (zr_plan_set): sequences
+// per CTA of the forward row and column passes and of the correlation column
+// and row passes.  A variant changes only how the work is split between
+// CTAs, never the arithmetic of a transform.  0 in the table means the
+// built-in default.
+enum TuneStage { TUNE_FWD_ROWS = 0, TUNE_FWD_COLS = 1, TUNE_XC_COLS = 2, TUNE_XC_ROWS = 3, TUNE_STAGES = 4 };
+int tune_get(int stage, int length);
+int tune_set(int stage, int length, int value);
 
 }  // namespace zr
 

@@ -230,6 +230,8 @@ using namespace zr;
 
 extern "C" int zr_shift_sum(const zr_frames_t* frames, const zr_shift_t* shifts, float* image_sum, float* even_sum,
                             float* odd_sum, float* aligned, void* stream) {
+  if (frames && frames->frame_movie)
+    return set_error(ZR_EINVAL, "zr_shift_sum: one movie at a time (frame_movie must be NULL)");
   if (!frames || !frames->raw || !shifts || !image_sum) return set_error(ZR_EINVAL, "zr_shift_sum: null argument");
   FrameSrc f = make_src(frames);
   if (f.N <= 0 || f.H < 2 || f.W < 2) return set_error(ZR_EINVAL, "zr_shift_sum: empty movie");

@@ -17,18 +17,14 @@
 namespace zr {
 
 constexpr int NBR = 4;  // rows per group of the row-pass output layout
-// rows per CTA of the row pass and columns per CTA of the column pass
-#ifndef ZR_FR_ROWS
-#define ZR_FR_ROWS 2
-#endif
-#ifndef ZR_FC_COLS
-#define ZR_FC_COLS 2
-#endif
-constexpr int FR = ZR_FR_ROWS, FC = ZR_FC_COLS;
+// rows per CTA of the row pass and columns per CTA of the column pass: the
+// defaults (two CTAs share an SM at 4096 points), or the planner's choice of
+// 1, 2 or 4 per transform length (tune_get)
+constexpr int FR_DEFAULT = 2, FC_DEFAULT = 2;
 // CTAs per SM to ask the register allocator for: 128 registers a thread
 constexpr int minb_of(int T) { return T >= 512 ? 1 : 512 / T; }
 
-template <int P1>
+template <int P1, int FR>
 __global__ void __launch_bounds__(fft_threads(P1, FR), minb_of(fft_threads(P1, FR)))
     k_fwd_rows(FrameSrc f, const float* __restrict__ mask, const double* __restrict__ mean_sub,
                double inv_area, int frame0, int mode, int rows, int cols, int C1, int K4, int H4,
@@ -43,7 +39,7 @@ __global__ void __launch_bounds__(fft_threads(P1, FR), minb_of(fft_threads(P1, F
   const int n = frame0 + nl;
   float mu = 0.0f;
   if (mode == 0 && mean_sub) mu = (float)(mean_sub[n] * inv_area);
-  if (mode == 0 && !mask && (f.fstride & 3) == 0) {
+  if (mode == 0 && !mask && (f.fstride & 3) == 0 && (f.mstride & 3) == 0) {
     // 4 pixels per thread and step: aligned vector loads of the raw frame and
     // every map; the unaligned head (< 4 pixels) and tail go pixel by pixel
     // FR_UNR quads per thread are fetched before any is used, so that several
@@ -149,7 +145,7 @@ __global__ void __launch_bounds__(fft_threads(P1, FR), minb_of(fft_threads(P1, F
   }
 }
 
-template <int P0>
+template <int P0, int FC>
 __global__ void __launch_bounds__(fft_threads(P0, FC), minb_of(fft_threads(P0, FC)))
     k_fwd_cols(const float2* __restrict__ RU, const float2* __restrict__ RV, int rows, int C0, int K4, int H4,
                long long spec_elems, float2* __restrict__ G, float2* __restrict__ S,
@@ -199,28 +195,51 @@ __global__ void k_frame_sums(FrameSrc f, double* __restrict__ sums) {
   }
 }
 
+template <int P, int FR>
+static int launch_rows_v(const FrameSrc& f, const float* mask, const double* mean_sub, double inv_area,
+                         int frame0, int nfr, int mode, int rows, int cols, int C1, int K4, int H4,
+                         float2* RU, float2* RV, const float2* tw, cudaStream_t st) {
+  constexpr int T = fft_threads(P, FR);
+  const size_t smem = (size_t)FR * ld_of(P) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_rows<P, FR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_fwd_rows attr"));
+  k_fwd_rows<P, FR><<<dim3(nfr, (rows + FR - 1) / FR), T, smem, st>>>(f, mask, mean_sub, inv_area, frame0, mode,
+                                                                       rows, cols, C1, K4, H4, RU, RV, tw);
+  return launched("k_fwd_rows");
+}
+
 template <int P>
 static int launch_rows(const FrameSrc& f, const float* mask, const double* mean_sub, double inv_area,
                        int frame0, int nfr, int mode, int rows, int cols, int C1, int K4, int H4,
                        float2* RU, float2* RV, const float2* tw, cudaStream_t st) {
-  constexpr int T = fft_threads(P, FR);
-  const size_t smem = (size_t)FR * ld_of(P) * sizeof(float2);
-  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_rows<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                    "k_fwd_rows attr"));
-  k_fwd_rows<P><<<dim3(nfr, (rows + FR - 1) / FR), T, smem, st>>>(f, mask, mean_sub, inv_area, frame0, mode, rows, cols, C1, K4,
-                                                 H4, RU, RV, tw);
-  return launched("k_fwd_rows");
+  switch (tune_get(TUNE_FWD_ROWS, P)) {
+    case 1: return launch_rows_v<P, 1>(f, mask, mean_sub, inv_area, frame0, nfr, mode, rows, cols, C1, K4, H4, RU, RV, tw, st);
+    case 4: return launch_rows_v<P, 4>(f, mask, mean_sub, inv_area, frame0, nfr, mode, rows, cols, C1, K4, H4, RU, RV, tw, st);
+    default:
+      return launch_rows_v<P, FR_DEFAULT>(f, mask, mean_sub, inv_area, frame0, nfr, mode, rows, cols, C1, K4, H4, RU,
+                                          RV, tw, st);
+  }
+}
+
+template <int P, int FC>
+static int launch_cols_v(const float2* RU, const float2* RV, int rows, int C0, int K4, int H4, long long se,
+                         int nfr, int nz, float2* G, float2* S, const float2* tw, cudaStream_t st) {
+  constexpr int T = fft_threads(P, FC);
+  const size_t smem = (size_t)FC * ld_of(P) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_cols<P, FC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_fwd_cols attr"));
+  k_fwd_cols<P, FC><<<dim3(K4 / FC, nfr, nz), T, smem, st>>>(RU, RV, rows, C0, K4, H4, se, G, S, tw);
+  return launched("k_fwd_cols");
 }
 
 template <int P>
 static int launch_cols(const float2* RU, const float2* RV, int rows, int C0, int K4, int H4, long long se,
                        int nfr, int nz, float2* G, float2* S, const float2* tw, cudaStream_t st) {
-  constexpr int T = fft_threads(P, FC);
-  const size_t smem = (size_t)FC * ld_of(P) * sizeof(float2);
-  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_fwd_cols<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                    "k_fwd_cols attr"));
-  k_fwd_cols<P><<<dim3(K4 / FC, nfr, nz), T, smem, st>>>(RU, RV, rows, C0, K4, H4, se, G, S, tw);
-  return launched("k_fwd_cols");
+  switch (tune_get(TUNE_FWD_COLS, P)) {
+    case 1: return launch_cols_v<P, 1>(RU, RV, rows, C0, K4, H4, se, nfr, nz, G, S, tw, st);
+    case 4: return launch_cols_v<P, 4>(RU, RV, rows, C0, K4, H4, se, nfr, nz, G, S, tw, st);
+    default: return launch_cols_v<P, FC_DEFAULT>(RU, RV, rows, C0, K4, H4, se, nfr, nz, G, S, tw, st);
+  }
 }
 
 #define ZR_POW2_DISPATCH(L, CALL)                  \
@@ -234,7 +253,8 @@ static int launch_cols(const float2* RU, const float2* RV, int rows, int C0, int
     case 2048: { constexpr int LL = 2048; CALL; } break; \
     case 3072: { constexpr int LL = 3072; CALL; } break; \
     case 4096: { constexpr int LL = 4096; CALL; } break; \
-    default: return set_error(ZR_ESIZE, "transform length %d not supported (powers of two 64..4096, 1536, 3072)", (int)(L)); \
+    case 6144: { constexpr int LL = 6144; CALL; } break; \
+    default: return set_error(ZR_ESIZE, "transform length %d not supported (powers of two 64..4096, 1536, 3072, 6144)", (int)(L)); \
   }
 
 }  // namespace zr
@@ -267,10 +287,10 @@ extern "C" int zr_spectra(const zr_frames_t* frames, const float* mask, const do
   if (!frames || !G || (mode == 0 && (!S || !frames->raw)))
     return set_error(ZR_EINVAL, "zr_spectra: null argument");
   if (!fft_len_ok(P0) || !fft_len_ok(P1) || !fft_len_ok(C0) || !fft_len_ok(C1) || C0 > P0 || C1 > P1 || C0 < 64 ||
-      C1 < 64)
+      C1 < 64 || P0 > 6144 || P1 > 6144 || C0 > 4096 || C1 > 4096)
     return set_error(ZR_ESIZE,
-                     "zr_spectra: P=%dx%d C=%dx%d must be powers of two or 3 x 2^k with 64 <= C <= P <= 4096", P0,
-                     P1, C0, C1);
+                     "zr_spectra: P=%dx%d C=%dx%d must be powers of two or 3 x 2^k with 64 <= C <= P, P <= 6144, "
+                     "C <= 4096", P0, P1, C0, C1);
   FrameSrc f = make_src(frames);
   if (f.H > P0 || f.W > P1) return set_error(ZR_EINVAL, "zr_spectra: frame %dx%d larger than padded %dx%d", f.H, f.W, P0, P1);
   if (n_frames <= 0 || frame0 < 0 || (mode == 0 && frame0 + n_frames > f.N))

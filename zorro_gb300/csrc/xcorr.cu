@@ -27,28 +27,24 @@
 
 namespace zr {
 
-// Column pass: columns per CTA (fewer for the long 3072 and 4096 columns)
-// and threads (ZR_XC_EPT elements per thread and pass).
-#ifndef ZR_XC_NBC
-#define ZR_XC_NBC 4
-#endif
+// Column pass: columns per CTA (by default fewer for the long 3072 and 4096
+// columns; the planner may choose 1, 2 or 4 per length) and threads
+// (ZR_XC_EPT elements per thread and pass).
 #ifndef ZR_XC_EPT
 #define ZR_XC_EPT 32
 #endif
 #ifndef ZR_XC_MINB
 #define ZR_XC_MINB 2
 #endif
-__host__ __device__ constexpr int xc_nbc(int C0) { return C0 >= 3072 ? 1 : ZR_XC_NBC; }
-__host__ __device__ constexpr int xc_threads(int C0) { return fft_threads(C0, xc_nbc(C0), ZR_XC_EPT); }
-// Row pass: packed row pairs per CTA, elements per thread and pass
-#ifndef ZR_XR_NBR
-#define ZR_XR_NBR 2
-#endif
+__host__ __device__ constexpr int xc_nbc_default(int C0) { return C0 >= 3072 ? 1 : 4; }
+__host__ __device__ constexpr int xc_threads(int C0, int NBC) { return fft_threads(C0, NBC, ZR_XC_EPT); }
+// Row pass: packed row pairs per CTA (default 2; the planner may choose 1,
+// 2 or 4), elements per thread and pass
 #ifndef ZR_XR_EPT
 #define ZR_XR_EPT 32
 #endif
-constexpr int XC_NBR = ZR_XR_NBR;
-__host__ __device__ constexpr int xr_threads(int C1) { return fft_threads(C1, XC_NBR, ZR_XR_EPT); }
+constexpr int XC_NBR_DEFAULT = 2;
+__host__ __device__ constexpr int xr_threads(int C1, int NBR) { return fft_threads(C1, NBR, ZR_XR_EPT); }
 __host__ __device__ constexpr int xr_minb(int T) { return T >= 512 ? 1 : 512 / T; }
 
 struct XcJobs {
@@ -123,18 +119,17 @@ __device__ __forceinline__ float2 xc_product(const E* a, const E* b, int row, in
   return h;
 }
 
-// Column pass: CTA (job, column group) transforms xc_nbc(C0) columns of the
+// Column pass: CTA (job, column group) transforms NBC columns of the
 // job's product.  Jobs vary fastest across the grid, so the CTAs resident at
 // one time read the same columns of every spectrum and share them through L2.
 // The first radix-16 pass forms the products while it loads its butterflies
 // from the (column-major) spectra, so no product buffer passes through shared
 // memory; the other passes run in shared memory, and the window rows
 // [-maxShift, ...) of the result are kept.
-template <int C0, typename E>
-__global__ void __launch_bounds__(xc_threads(C0), ZR_XC_MINB)
+template <int C0, typename E, int NBC>
+__global__ void __launch_bounds__(xc_threads(C0, NBC), ZR_XC_MINB)
     k_xc_cols(XcJobs J, int C1, int K4, int mS, float2* __restrict__ Tw, const float2* __restrict__ tw) {
-  constexpr int NBC = xc_nbc(C0);
-  constexpr int T = xc_threads(C0);
+  constexpr int T = xc_threads(C0, NBC);
   constexpr int LD = ld_of(C0);
   constexpr int RP = C0 + 4;  // column pitch of the spectra
   constexpr int R = fft_radix(C0);
@@ -203,11 +198,11 @@ __global__ void __launch_bounds__(xc_threads(C0), ZR_XC_MINB)
   }
 }
 
-template <int C1>
-__global__ void __launch_bounds__(xr_threads(C1), xr_minb(xr_threads(C1)))
+template <int C1, int XC_NBR>
+__global__ void __launch_bounds__(xr_threads(C1, XC_NBR), xr_minb(xr_threads(C1, XC_NBR)))
     k_xc_rows(XcJobs J, int C0, int K4, int mS, float scale, const float2* __restrict__ Tw,
               const float* __restrict__ terms, float* __restrict__ out, const float2* __restrict__ tw) {
-  constexpr int T = xr_threads(C1);
+  constexpr int T = xr_threads(C1, XC_NBR);
   constexpr int LD = ld_of(C1);
   extern __shared__ float2 sm[];
   const int w = 2 * mS;
@@ -256,35 +251,55 @@ __global__ void __launch_bounds__(xr_threads(C1), xr_minb(xr_threads(C1)))
   }
 }
 
-template <int C0, typename E>
+template <int C0, typename E, int NBC>
 static int launch_xc_cols_t(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
                             cudaStream_t st) {
-  constexpr int T = xc_threads(C0);
-  constexpr int NBC = xc_nbc(C0);
+  constexpr int T = xc_threads(C0, NBC);
   const size_t smem = (size_t)NBC * ld_of(C0) * sizeof(float2);
-  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                    "k_xc_cols attr"));
-  k_xc_cols<C0, E><<<dim3(nj, K4 / NBC), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_cols<C0, E, NBC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem), "k_xc_cols attr"));
+  k_xc_cols<C0, E, NBC><<<dim3(nj, K4 / NBC), T, smem, st>>>(J, C1, K4, mS, Tw, tw);
   return launched("k_xc_cols");
+}
+
+template <int C0, typename E>
+static int launch_xc_cols_e(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
+                            cudaStream_t st) {
+  switch (tune_get(TUNE_XC_COLS, C0)) {
+    case 1: return launch_xc_cols_t<C0, E, 1>(J, nj, C1, K4, mS, Tw, tw, st);
+    case 2: return launch_xc_cols_t<C0, E, 2>(J, nj, C1, K4, mS, Tw, tw, st);
+    case 4: return launch_xc_cols_t<C0, E, 4>(J, nj, C1, K4, mS, Tw, tw, st);
+    default: return launch_xc_cols_t<C0, E, xc_nbc_default(C0)>(J, nj, C1, K4, mS, Tw, tw, st);
+  }
 }
 
 template <int C0>
 static int launch_xc_cols(const XcJobs& J, int nj, int C1, int K4, int mS, float2* Tw, const float2* tw,
                           cudaStream_t st) {
-  if (J.sc) return launch_xc_cols_t<C0, __half2>(J, nj, C1, K4, mS, Tw, tw, st);
-  return launch_xc_cols_t<C0, float2>(J, nj, C1, K4, mS, Tw, tw, st);
+  if (J.sc) return launch_xc_cols_e<C0, __half2>(J, nj, C1, K4, mS, Tw, tw, st);
+  return launch_xc_cols_e<C0, float2>(J, nj, C1, K4, mS, Tw, tw, st);
+}
+
+template <int C1, int NBR>
+static int launch_xc_rows_v(const XcJobs& J, int nj, int C0, int K4, int mS, float scale, const float2* Tw,
+                            const float* terms, float* out, const float2* tw, cudaStream_t st) {
+  constexpr int T = xr_threads(C1, NBR);
+  const size_t smem = (size_t)NBR * ld_of(C1) * sizeof(float2);
+  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_rows<C1, NBR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "k_xc_rows attr"));
+  k_xc_rows<C1, NBR><<<dim3((J.rows + 2 * NBR - 1) / (2 * NBR), nj), T, smem, st>>>(J, C0, K4, mS, scale, Tw,
+                                                                                   terms, out, tw);
+  return launched("k_xc_rows");
 }
 
 template <int C1>
 static int launch_xc_rows(const XcJobs& J, int nj, int C0, int K4, int mS, float scale, const float2* Tw,
                           const float* terms, float* out, const float2* tw, cudaStream_t st) {
-  constexpr int T = xr_threads(C1);
-  const size_t smem = (size_t)XC_NBR * ld_of(C1) * sizeof(float2);
-  ZR_TRY(cuda_check(cudaFuncSetAttribute(k_xc_rows<C1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                    "k_xc_rows attr"));
-  k_xc_rows<C1><<<dim3((J.rows + 2 * XC_NBR - 1) / (2 * XC_NBR), nj), T, smem, st>>>(J, C0, K4, mS, scale, Tw,
-                                                                                    terms, out, tw);
-  return launched("k_xc_rows");
+  switch (tune_get(TUNE_XC_ROWS, C1)) {
+    case 1: return launch_xc_rows_v<C1, 1>(J, nj, C0, K4, mS, scale, Tw, terms, out, tw, st);
+    case 4: return launch_xc_rows_v<C1, 4>(J, nj, C0, K4, mS, scale, Tw, terms, out, tw, st);
+    default: return launch_xc_rows_v<C1, XC_NBR_DEFAULT>(J, nj, C0, K4, mS, scale, Tw, terms, out, tw, st);
+  }
 }
 
 #define ZR_XC_DISPATCH(L, CALL)                               \

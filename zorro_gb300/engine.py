@@ -26,6 +26,7 @@ import contextlib
 import ctypes as C
 import threading
 import time
+import types
 
 import numpy as np
 
@@ -40,9 +41,12 @@ _PEAK_DTYPE = np.dtype([("sy", "f8"), ("sx", "f8"), ("sigma", "f8"), ("corr", "f
 _RAW_TYPES = {np.dtype(np.float32): _lib.ZR_F32, np.dtype(np.uint8): _lib.ZR_U8, np.dtype(np.uint16): _lib.ZR_U16,
               np.dtype(np.float16): _lib.ZR_F16}
 
-# scratch budgets (bytes) for the staged passes
+# scratch budgets (bytes) for the staged passes.  The pair stage runs its
+# jobs in waves that fit XCORR_WORK, and every wave reads the spectra of all
+# frames again: 1.5 GB holds the 780 pairs of a 40-frame K2 movie (1.6 MB of
+# column-pass output each at crop 2048, maxShift 100) in one wave.
 SPECTRA_WORK = 512 << 20
-XCORR_WORK = 256 << 20
+XCORR_WORK = 1536 << 20
 DOSE_WORK = 1536 << 20
 
 
@@ -51,7 +55,7 @@ def _crop_ok(v):
 
 
 def _padded_ok(v):
-    return (_pow2(v) and 64 <= v <= 4096) or v in (1536, 3072)
+    return (_pow2(v) and 64 <= v <= 4096) or v in (1536, 3072, 6144)
 
 
 _CROP_OK, _PADDED_OK = _crop_ok, _padded_ok
@@ -83,6 +87,9 @@ class Engine:
             _lib.call("zr_init", device)
         self._slots = {}
         self._slots_lock = threading.Lock()
+        self._planned = set()
+        self._plan_lock = threading.Lock()
+        self.last_plan = None
         self._tls = threading.local()
         self.profile = None  # dict stage -> list of (start, end) CUDA events when enabled
         self._profile_lock = threading.Lock()
@@ -106,6 +113,59 @@ class Engine:
         """Summed device time per stage of the recorded calls (synchronises)."""
         self.torch.cuda.synchronize(self.dev)
         return {k: sum(a.elapsed_time(b) for a, b in v) for k, v in (self.profile or {}).items()}
+
+    # ------------------------------------------------------------------ planning
+    def plan(self, P0, P1, C0, C1, mS, effort="FFTW_MEASURE", cache_dir=None):
+        """Launch variants of the transform kernels for one registration shape
+        (pyFFTWPlanner's FFTW_MEASURE planning and wisdom,
+        zorro_util.py:966-1066): the choice saved in ``cache_dir``'s plan file
+        for this GPU model and library version, or measured now by zr_plan
+        and saved there.  'FFTW_ESTIMATE' keeps the built-in variants.  Done
+        once per shape and engine; the variants change no result."""
+        import json
+        import os
+        import tempfile
+        if str(effort).upper() == "FFTW_ESTIMATE":
+            return None
+        key = (P0, P1, C0, C1, mS)
+        with self._plan_lock:
+            if key in self._planned:
+                return None
+            torch = self.torch
+            shape = _lib.PlanShape(P0, P1, C0, C1, mS, 8)
+            choice = _lib.PlanChoice()
+            path = os.path.join(cache_dir or tempfile.gettempdir(), "zorro_gb300_plans.json")
+            name = "%s|lib%d|P%dx%d|C%dx%d|m%d" % (torch.cuda.get_device_name(self.device), self.lib.zr_version(),
+                                                   P0, P1, C0, C1, mS)
+            try:
+                with open(path) as fh:
+                    wisdom = json.load(fh)
+            except (OSError, ValueError):
+                wisdom = {}
+            saved = wisdom.get(name)
+            if saved:
+                choice.fwd_rows, choice.fwd_cols, choice.xc_cols, choice.xc_rows = (int(v) for v in saved["choice"])
+                _lib.call("zr_plan_set", C.byref(shape), C.byref(choice))
+            else:
+                wb = self.lib.zr_plan_work_bytes(C.byref(shape))
+                work = torch.empty(max(int(wb), 1), dtype=torch.uint8, device=self.dev)
+                with torch.cuda.device(self.dev):
+                    _lib.call("zr_plan", C.byref(shape), work.data_ptr(), wb,
+                              torch.cuda.current_stream(self.dev).cuda_stream, C.byref(choice))
+                del work
+                wisdom[name] = {"choice": [choice.fwd_rows, choice.fwd_cols, choice.xc_cols, choice.xc_rows],
+                                "ms_spectra": [list(r) for r in choice.ms_spectra],
+                                "ms_pairs": [list(r) for r in choice.ms_pairs]}
+                try:
+                    tmp = "%s.%d.tmp" % (path, os.getpid())
+                    with open(tmp, "w") as fh:
+                        json.dump(wisdom, fh, indent=1, sort_keys=True)
+                    os.replace(tmp, path)
+                except OSError:
+                    pass  # an unwritable cache directory only costs the next process a measurement
+            self._planned.add(key)
+            self.last_plan = (name, [choice.fwd_rows, choice.fwd_cols, choice.xc_cols, choice.xc_rows])
+            return self.last_plan
 
     # ------------------------------------------------------------------ slots and buffers
     def _slot(self, slot, priority=0):
@@ -156,7 +216,7 @@ class Engine:
         return self.torch.cuda.current_stream(self.dev).cuda_stream
 
     # ------------------------------------------------------------------ input
-    def upload(self, reg):
+    def upload(self, reg, pfx=""):
         torch = self.torch
         imgs = reg.images
         from .mrc import Packed4
@@ -165,9 +225,9 @@ class Engine:
             # expands them into the uint8 frames the kernels read
             N, H, W = imgs.shape
             src = torch.from_numpy(np.ascontiguousarray(imgs.data).reshape(-1))
-            packed = self.buf("u4packed", src.numel())[:src.numel()]
+            packed = self.buf(pfx + "u4packed", src.numel())[:src.numel()]
             packed.copy_(src, non_blocking=True)
-            imgs = self.tensor("u4frames", (N, H, W), torch.uint8)
+            imgs = self.tensor(pfx + "u4frames", (N, H, W), torch.uint8)
             self.call("A_gain_sum", "zr_unpack_u4", packed.data_ptr(), N, H, W, imgs.data_ptr(), self.stream)
         if isinstance(imgs, torch.Tensor):
             t = imgs.to(self.dev, non_blocking=True)
@@ -233,7 +293,6 @@ class Engine:
         registrations' error dictionaries ({'even': ..., 'odd': ...}; the
         reference discards its half-set registrators, this keeps their pair
         measurements for inspection)."""
-        from .registrator import ImageRegistrator, copy_config
         torch = self.torch
         N, H, W = (int(v) for v in aligned.shape)
         if N < 2:
@@ -246,22 +305,7 @@ class Engine:
         parent = self._tls.slot["key"]
 
         def register(images, sub_slot, after_hot=None, start=None, **kw):
-            r = ImageRegistrator()
-            copy_config(reg, r)
-            r.images = images
-            r.gainRef = None
-            r.masks = None
-            r.gain = None
-            r.doEvenOddFRC = False
-            r.doLazyFRC = False
-            r.filterMode = "hot" if "hot" in filt else None
-            r.hotpixInfo = dict(hotinfo)
-            r.keepAlignedImages = False
-            r.returnDeviceArrays = True
-            r.errorDictList = []
-            r.bench = {}
-            for k, v in kw.items():
-                setattr(r, k, v)
+            r = self._half_set_reg(reg, images, hotinfo, filt, **kw)
             if start is not None:
                 start.wait()
             # the half sets are on the critical path, the parent's dose filter
@@ -292,6 +336,38 @@ class Engine:
         with torch.cuda.stream(self._slot(("halfset_even", parent), priority=-1)["stream"]):
             pair = torch.stack([ev.imageSum, od.imageSum])
         eo = register(pair, ("halfset_even", parent), triMode="first", keepAlignedImages=True)
+        return self._pair_frc(ev, od, eo, H, W)
+
+    @staticmethod
+    def _half_set_reg(reg, images, hotinfo, filt, **kw):
+        """A registrator for one half set of the even/odd FRC (or for the pair
+        of half sums): the parent's settings, its fitted hot-pixel settings,
+        no FRC and no dose filter of its own, outputs left on the device."""
+        from .registrator import ImageRegistrator, copy_config
+        r = ImageRegistrator()
+        copy_config(reg, r)
+        r.images = images
+        r.gainRef = None
+        r.masks = None
+        r.gain = None
+        r.doEvenOddFRC = False
+        r.doLazyFRC = False
+        r.filterMode = "hot" if "hot" in filt else None
+        r.hotpixInfo = dict(hotinfo)
+        r.keepAlignedImages = False
+        r.returnDeviceArrays = True
+        r.errorDictList = []
+        r.bench = {}
+        for k, v in kw.items():
+            setattr(r, k, v)
+        return r
+
+    def _pair_frc(self, ev, od, eo, H, W, pfx=""):
+        """The tiled FRC of the aligned pair of half sums (``eo``, registered in
+        triMode 'first') with the crop limits of hstack([transEven,
+        transOdd]).  Returns FRC, FRC2D, transEven, transOdd and the half-set
+        error dictionaries."""
+        torch = self.torch
         te, to = np.asarray(ev.translations), np.asarray(od.translations)
         box = 512
         offs, tiles = hm.frc_tiles((H, W), np.hstack([te, to]))
@@ -304,11 +380,81 @@ class Engine:
         pair = eo.images.contiguous()
         offs_dev = torch.from_numpy(offs.reshape(-1)).to(self.dev, non_blocking=True)
         fwb = self.lib.zr_frc_work_bytes(len(offs), box)
-        f2 = self.tensor("frc2d", (box, box), torch.float32)
-        fr = self.tensor("frc_eo", (nr,), torch.float64)
+        f2 = self.tensor(pfx + "frc2d", (box, box), torch.float32)
+        fr = self.tensor(pfx + "frc_eo", (nr,), torch.float64)
         self.call("H_frc", "zr_tiled_frc", pair[0].data_ptr(), pair[1].data_ptr(), H, W, box, offs_dev.data_ptr(),
-                  len(offs), f2.data_ptr(), fr.data_ptr(), nr, self.ptr("frcwork", fwb), fwb, self.stream)
+                  len(offs), f2.data_ptr(), fr.data_ptr(), nr, self.ptr(pfx + "frcwork", fwb), fwb, self.stream)
         return fr, f2, te, to, halves
+
+    # ------------------------------------------------------------------ batches of movies
+    def align_batch(self, regs, slot=0):
+        """Register several movies, of any detector sizes and frame counts,
+        with shared launches (all outputs set on each registrator).
+
+        Each movie is prepared on its own (upload, Fourier binning, hot-pixel
+        filter); movies of the same shape class (frame shape, pixel type,
+        corrections, transform sizes, peak search: ``batch_key``) then share
+        one set of launches for the forward spectra, the frame terms, the
+        correlation windows of every pair and their peak search, their frames
+        concatenated and each frame reading its own movie's maps.  Each movie
+        is then solved, shifted and filtered; the half sets of every movie's
+        even/odd FRC are registered as one more batch, and the pairs of their
+        sums as another.  The results equal each movie registered alone
+        (the same kernels on the same values; tested)."""
+        torch = self.torch
+        st = self._slot(slot)
+        prev = getattr(self._tls, "slot", None)
+        self._tls.slot = st
+        try:
+            sctx = torch.cuda.stream(st["stream"]) if st["stream"] is not None else contextlib.nullcontext()
+            with torch.cuda.device(self.dev), sctx:
+                outs = self._align_batch(regs, "b")
+                if st["stream"] is not None:
+                    st["stream"].synchronize()
+        finally:
+            self._tls.slot = prev
+        for reg, res in zip(regs, outs):
+            for k, v in res.items():
+                setattr(reg, k, v)
+
+    def _align_batch(self, regs, tag):
+        jobs = [self._prepare(r, pfx="%s%d_" % (tag, i)) for i, r in enumerate(regs)]
+        classes = {}
+        for j in jobs:
+            key = self.batch_key(j)
+            classes.setdefault(key if key is not None else ("alone", j.pfx), []).append(j)
+        for ci, js in enumerate(classes.values()):
+            self._correlate(js, cls="%sc%d_" % (tag, ci))
+        outs = [self._finish_main(j) for j in jobs]
+        eo = [j for j in jobs if j.reg.doEvenOddFRC]
+        halves = dict(zip((j.pfx for j in eo), self._even_odd_batch(eo, tag))) if eo else {}
+        return [self._finish_out(j, out, halves.get(j.pfx)) for j, out in zip(jobs, outs)]
+
+    def _even_odd_batch(self, jobs, tag):
+        """The independent even/odd FRC of several movies: every movie's even
+        and odd half sets registered as one batch, the pairs of half sums as
+        another, then each movie's tiled FRC (as _even_odd_frc does for one)."""
+        torch = self.torch
+        halves = []
+        for j in jobs:
+            if j.N < 2:
+                raise ValueError("doEvenOddFRC needs at least two frames")
+            halves.append(self._half_set_reg(j.reg, j.aligned[0::2], j.hotinfo, j.filt))
+            halves.append(self._half_set_reg(j.reg, j.aligned[1::2], j.hotinfo, j.filt))
+        self._set_outputs(halves, self._align_batch(halves, tag + "h"))
+        pairs = []
+        for k, j in enumerate(jobs):
+            pair = torch.stack([halves[2 * k].imageSum, halves[2 * k + 1].imageSum])
+            pairs.append(self._half_set_reg(j.reg, pair, j.hotinfo, j.filt, triMode="first", keepAlignedImages=True))
+        self._set_outputs(pairs, self._align_batch(pairs, tag + "f"))
+        return [self._pair_frc(halves[2 * k], halves[2 * k + 1], pairs[k], j.H, j.W, pfx=j.pfx)
+                for k, j in enumerate(jobs)]
+
+    @staticmethod
+    def _set_outputs(regs, outs):
+        for reg, res in zip(regs, outs):
+            for k, v in res.items():
+                setattr(reg, k, v)
 
     def _frames(self, raw, rtype, gain, ha=None, hb=None, gdiv=0.0):
         N, H, W = raw.shape
@@ -516,6 +662,15 @@ class Engine:
         return pr, keep
 
     def _align(self, reg):
+        """One movie: prepare, correlate, solve, shift, filter, FRC."""
+        job = self._prepare(reg)
+        self._correlate([job])
+        return self._finish(job)
+
+    def _prepare(self, reg, pfx=""):
+        """Upload, Fourier binning, hot-pixel filter, padded and crop sizes,
+        mask and per-frame mean of one movie.  Returns the movie's job state;
+        ``pfx`` keeps its buffers apart from the other movies of a batch."""
         torch = self.torch
         st = self.stream
         bench = {}
@@ -525,7 +680,7 @@ class Engine:
             # that shift method needs (self.__sC2 is undefined, zorro.py:891-895)
             raise AttributeError("shiftMethod 'fourier' is broken in the reference: self.__sC2 is undefined "
                                  "(zorro.py:895)")
-        raw, gain, rtype = self.upload(reg)
+        raw, gain, rtype = self.upload(reg, pfx)
         N, H, W = (int(s) for s in raw.shape)
         raw_float = bool(getattr(reg, "imagesAreRaw", False))
         gdiv = float(reg.gain) if (reg.gain and not np.isclose(reg.gain, 1.0) and (rtype != _lib.ZR_F32 or raw_float)) \
@@ -536,9 +691,9 @@ class Engine:
             # binStack (zorro.py:1826-1904), before the hot-pixel filter as there
             Hb, Wb = int(reg.shapeBinned[0]), int(reg.shapeBinned[1])
             bwb = self.lib.zr_bin_work_bytes(H, W, Hb, Wb)
-            binned = self.tensor("binned", (N, Hb, Wb), torch.float32)
+            binned = self.tensor(pfx + "binned", (N, Hb, Wb), torch.float32)
             self.call("A_gain_sum", "zr_bin_fourier", C.byref(frames), Hb, Wb, binned.data_ptr(),
-                      self.ptr("binwork", bwb), bwb, st)
+                      self.ptr(pfx + "binwork", bwb), bwb, st)
             scale = np.array([H, W], dtype=np.float64) / np.array([Hb, Wb], dtype=np.float64)
             if pixelsize is not None:
                 pixelsize = pixelsize * np.mean(scale)
@@ -552,13 +707,13 @@ class Engine:
         ha = hb = None
         if "hot" in filt:
             bench["hot0"] = time.time()
-            usum = self.tensor("usum", (H, W), torch.float32)
-            tot = self.tensor("tot", (4,), torch.float64)
+            usum = self.tensor(pfx + "usum", (H, W), torch.float32)
+            tot = self.tensor(pfx + "tot", (4,), torch.float64)
             tot.zero_()
             self.call("A_gain_sum", "zr_gain_sum", C.byref(frames), usum.data_ptr(), tot.data_ptr(), st)
             sumMean, pstd, edges = hm.hotpix_bins(float(tot[0].item()) / (H * W), hotinfo["maxSigma"])
             nb = len(edges) - 1
-            hist = self.tensor("hist", (nb + 4,), torch.int32)
+            hist = self.tensor(pfx + "hist", (nb + 4,), torch.int32)
             hist.zero_()
             self.call("A_gain_sum", "zr_histogram", usum.data_ptr(), H * W, float(edges[0]), nb, hist.data_ptr(), st)
             h = hist[:nb].cpu().numpy().astype(np.int64)
@@ -573,13 +728,13 @@ class Engine:
                 prm.psf[i] = float(psf[i])
             prm.neighbour_thres = 0.01
             prm.best_mean = float(mu / N)
-            ha = self.tensor("hot_a", (H, W), torch.float32)
-            hb = self.tensor("hot_b", (H, W), torch.float32)
-            cnt = self.tensor("hotcnt", (4,), torch.int32)
+            ha = self.tensor(pfx + "hot_a", (H, W), torch.float32)
+            hb = self.tensor(pfx + "hot_b", (H, W), torch.float32)
+            cnt = self.tensor(pfx + "hotcnt", (4,), torch.int32)
             cnt.zero_()
             wb = self.lib.zr_hotpix_work_bytes(H, W)
             self.call("B_hot_maps", "zr_hotpix_maps", usum.data_ptr(), H, W, N, C.byref(prm), ha.data_ptr(), hb.data_ptr(),
-                      cnt.data_ptr(), self.ptr("hotwork", wb), wb, st)
+                      cnt.data_ptr(), self.ptr(pfx + "hotwork", wb), wb, st)
             c = cnt.cpu().numpy()
             hotinfo["guessDeadpix"] = int(c[0])
             hotinfo["guessHotpix"] = int(c[1])
@@ -607,10 +762,12 @@ class Engine:
         for v, nm, ok in ((P0, "shapePadded", _PADDED_OK), (P1, "shapePadded", _PADDED_OK), (C0, "fouCrop", _CROP_OK),
                           (C1, "fouCrop", _CROP_OK)):
             if not ok(v):
-                raise ValueError("%s %d: the GPU path transforms powers of two (64..4096) and 1536, 3072 (padded) or "
-                                 "384, 768, 1536, 3072 (crop)" % (nm, v))
+                raise ValueError("%s %d: the GPU path transforms powers of two (64..4096) and 1536, 3072, 6144 "
+                                 "(padded) or 384, 768, 1536, 3072 (crop)" % (nm, v))
         mS = int(reg.maxShift)
         w = 2 * mS
+        if 2 <= mS and 2 * mS <= min(C0, C1):
+            self.plan(P0, P1, C0, C1, mS, getattr(reg, "fftw_effort", "FFTW_MEASURE"), getattr(reg, "cachePath", None))
         mask_dev = None
         user_mask = reg.masks is not None and len(np.shape(reg.masks)) > 0
         if user_mask:
@@ -623,7 +780,7 @@ class Engine:
             mask_dev = torch.from_numpy(mp).to(self.dev, non_blocking=True)
         msub = None
         if reg.subtractFrameMean and not user_mask:
-            msub = self.tensor("msub", (N,), torch.float64)
+            msub = self.tensor(pfx + "msub", (N,), torch.float64)
             if "hot" in filt:
                 # any per-frame constant is exact; the mean frame of the unaligned
                 # sum is close to every frame's mean and costs no extra pass
@@ -631,59 +788,24 @@ class Engine:
             else:
                 msub.zero_()
                 self.call("C_spectra", "zr_frame_sums", C.byref(frames), msub.data_ptr(), st)
-
-        # ---- spectra (xcorrnm2_tri zorro.py:814-925)
-        bench["xcorr0"] = time.time()
-        se = int(self.lib.zr_spectrum_elems(C0, C1))
-        half = str(getattr(reg, "spectraPrecision", "float32")).lower() in ("float16", "half", "f16")
-        if half and reg.triMode == "refine":
+        job = types.SimpleNamespace(
+            reg=reg, pfx=pfx, bench=bench, raw=raw, gain=gain, rtype=rtype, gdiv=gdiv, N=N, H=H, W=W, frames=frames,
+            pixelsize=pixelsize, hotinfo=hotinfo, filt=filt, ha=ha, hb=hb, P0=P0, P1=P1, C0=C0, C1=C1, mS=mS, w=w,
+            mask_dev=mask_dev, user_mask=user_mask, msub=msub,
+            half=str(getattr(reg, "spectraPrecision", "float32")).lower() in ("float16", "half", "f16"),
+            refine=reg.triMode == "refine", preshift=bool(reg.preShift and mS))
+        if job.half and job.refine:
             raise ValueError("triMode 'refine' builds its templates from float32 spectra (spectraPrecision 'float32')")
-        mrows = P0 if mask_dev is not None else H
-        wbm = self.lib.zr_spectra_work_bytes(mrows, 1, C1)
-        per = self.lib.zr_spectra_work_bytes(H, 1, C1)
-        chunk = max(1, min(N, SPECTRA_WORK // per))
-        if half:
-            # half-precision store with per-spectrum power-of-two scales: each
-            # chunk of frames goes through a float32 staging buffer, then packed
-            G16 = self.tensor("G16", (N, se), torch.int32)
-            S16 = self.tensor("S16", (N, se), torch.int32)
-            GM16 = self.tensor("GM16", (se,), torch.int32)
-            hsc = self.tensor("hscales", (2 * N + 1,), torch.float32)
-            pw = self.ptr("packwork", 4 * max(N, 1))
-            G = self.tensor("G", (chunk, se, 2), torch.float32)
-            S = self.tensor("S", (chunk, se, 2), torch.float32)
-        else:
-            G = self.tensor("G", (N, se, 2), torch.float32)
-            S = self.tensor("S", (N, se, 2), torch.float32)
-        GM = self.tensor("GM", (se, 2), torch.float32)
-        self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None, None, 0, 1,
-                  1, P0, P1, C0, C1, GM.data_ptr(), None, self.ptr("specwork", wbm), wbm, st)
-        if half:
-            self.call("C_spectra", "zr_pack_half", GM.data_ptr(), 1, se, GM16.data_ptr(), hsc[2 * N:].data_ptr(),
-                      pw, 4 * N, st)
-        wb = per * chunk
-        wptr = self.ptr("specwork", wb)
-        for f0 in range(0, N, chunk):
-            nf = min(chunk, N - f0)
-            g0 = 0 if half else f0
-            self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None,
-                      msub.data_ptr() if msub is not None else None, f0, nf, 0, P0, P1, C0, C1,
-                      G[g0].data_ptr(), S[g0].data_ptr(), wptr, wb, st)
-            if half:
-                self.call("C_spectra", "zr_pack_half", G.data_ptr(), nf, se, G16[f0].data_ptr(), hsc[f0:].data_ptr(),
-                          pw, 4 * N, st)
-                self.call("C_spectra", "zr_pack_half", S.data_ptr(), nf, se, S16[f0].data_ptr(),
-                          hsc[N + f0:].data_ptr(), pw, 4 * N, st)
-
-        # ---- correlation windows and peaks (mnxc2 / locatePeak)
-        refine = reg.triMode == "refine"
-        if refine:
+        if job.refine:
             # frame I against the template of the others, I < N-1 (zorro.py:941-954)
-            pairs = np.array([(I, I) for I in range(N - 1)], dtype=np.int32).reshape(-1, 2)
+            job.pairs = np.array([(I, I) for I in range(N - 1)], dtype=np.int32).reshape(-1, 2)
         else:
-            tri = hm.tri_indices(N, reg.triMode, reg.diagWidth, reg.diagStart)
-            pairs = hm.pair_list(tri)
-        M = len(pairs)
+            job.pairs = hm.pair_list(hm.tri_indices(N, reg.triMode, reg.diagWidth, reg.diagStart))
+        job.pp = self._peak_params(reg, P0, P1)
+        return job
+
+    def _peak_params(self, reg, P0, P1):
+        """locatePeak's settings (zorro.py:1099-1231) as zr_peak_params_t."""
         pp = PeakParams()
         pp.sub_pix_reg = int(reg.subPixReg or 1)
         bm = str(reg.Bmode)
@@ -700,22 +822,197 @@ class Engine:
         pp.suppress_origin = int(bool(reg.suppressOrigin))
         pp.use_mask = 1
         pp.opti_lo, pp.opti_hi, pp.opti_xatol, pp.opti_maxiter = 0.0, 7.0, 0.01, 15
-        spec = (half, G, S, GM, G16 if half else None, S16 if half else None, GM16 if half else None,
-                hsc if half else None)
-        if reg.preShift and mS:
-            pr, keep = self._preshift(reg, pairs, refine, N, C0, C1, pp, spec, st)
+        return pp
+
+    # ------------------------------------------------------------------ spectra and pairs
+    def _correlate(self, jobs, cls=""):
+        """Forward spectra, frame terms, correlation windows and peaks
+        (xcorrnm2_tri, mnxc2, locatePeak) of one movie, or of several movies
+        of one shape class in one set of launches: their frames concatenated
+        (each frame reading its own movie's gain and hot-pixel maps), the
+        frame terms of all frames, every movie's pairs with its frames'
+        offsets, and all windows' peaks.  Sets each job's ``pr`` and ``keep``."""
+        for j in jobs:
+            j.bench["xcorr0"] = time.time()
+        if len(jobs) == 1:
+            self._correlate_one(jobs[0])
         else:
-            pr = self._cropped_peaks(reg, pairs, refine, N, C0, C1, mS, pp, spec, st)
-            keep = np.ones(M, dtype=bool)
-            if reg.triMode == "auto":
+            self._correlate_batch(jobs, cls)
+        for j in jobs:
+            reg = j.reg
+            keep = j.keep
+            if not j.preshift and reg.triMode == "auto":
                 row_done = {}
-                for k, (I, J) in enumerate(pairs):
+                for k, (I, J) in enumerate(j.pairs):
                     if row_done.get(I):
                         keep[k] = False
                         continue
-                    if pr["peaksig"][k] <= reg.peaksigThres or J - I >= reg.autoMax:
+                    if j.pr["peaksig"][k] <= reg.peaksigThres or J - I >= reg.autoMax:
                         row_done[I] = True
-        bench["xcorr2"] = time.time()
+            j.bench["xcorr2"] = time.time()
+
+    def _spectra_pass(self, frames, mask_dev, msub, N, H, P0, P1, C0, C1, G, S, pfx, half=None):
+        """zr_spectra over frames [0, N) in chunks that fit SPECTRA_WORK;
+        ``half`` = (G16, S16, hsc, packwork) packs each chunk to half
+        precision (G and S are then one chunk long)."""
+        st = self.stream
+        per = self.lib.zr_spectra_work_bytes(H, 1, C1)
+        chunk = max(1, min(N, SPECTRA_WORK // per))
+        wb = per * chunk
+        wptr = self.ptr(pfx + "specwork", wb)
+        se = int(self.lib.zr_spectrum_elems(C0, C1))
+        for f0 in range(0, N, chunk):
+            nf = min(chunk, N - f0)
+            g0 = 0 if half else f0
+            self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None,
+                      msub.data_ptr() if msub is not None else None, f0, nf, 0, P0, P1, C0, C1,
+                      G[g0].data_ptr(), S[g0].data_ptr(), wptr, wb, st)
+            if half:
+                G16, S16, hsc, pw = half
+                self.call("C_spectra", "zr_pack_half", G.data_ptr(), nf, se, G16[f0].data_ptr(), hsc[f0:].data_ptr(),
+                          pw, 4 * N, st)
+                self.call("C_spectra", "zr_pack_half", S.data_ptr(), nf, se, S16[f0].data_ptr(),
+                          hsc[N + f0:].data_ptr(), pw, 4 * N, st)
+
+    def _mask_spectrum(self, frames, mask_dev, H, P0, P1, C0, C1, pfx):
+        torch = self.torch
+        se = int(self.lib.zr_spectrum_elems(C0, C1))
+        GM = self.tensor(pfx + "GM", (se, 2), torch.float32)
+        mrows = P0 if mask_dev is not None else H
+        wbm = self.lib.zr_spectra_work_bytes(mrows, 1, C1)
+        self.call("C_spectra", "zr_spectra", C.byref(frames), mask_dev.data_ptr() if mask_dev is not None else None,
+                  None, 0, 1, 1, P0, P1, C0, C1, GM.data_ptr(), None, self.ptr(pfx + "specwork", wbm), wbm,
+                  self.stream)
+        return GM
+
+    def _correlate_one(self, job):
+        torch = self.torch
+        st = self.stream
+        reg, pfx = job.reg, job.pfx
+        N, H, P0, P1, C0, C1 = job.N, job.H, job.P0, job.P1, job.C0, job.C1
+        se = int(self.lib.zr_spectrum_elems(C0, C1))
+        per = self.lib.zr_spectra_work_bytes(H, 1, C1)
+        chunk = max(1, min(N, SPECTRA_WORK // per))
+        half = job.half
+        G16 = S16 = GM16 = hsc = None
+        if half:
+            # half-precision store with per-spectrum power-of-two scales: each
+            # chunk of frames goes through a float32 staging buffer, then packed
+            G16 = self.tensor(pfx + "G16", (N, se), torch.int32)
+            S16 = self.tensor(pfx + "S16", (N, se), torch.int32)
+            GM16 = self.tensor(pfx + "GM16", (se,), torch.int32)
+            hsc = self.tensor(pfx + "hscales", (2 * N + 1,), torch.float32)
+            pw = self.ptr(pfx + "packwork", 4 * max(N, 1))
+            G = self.tensor(pfx + "G", (chunk, se, 2), torch.float32)
+            S = self.tensor(pfx + "S", (chunk, se, 2), torch.float32)
+        else:
+            G = self.tensor(pfx + "G", (N, se, 2), torch.float32)
+            S = self.tensor(pfx + "S", (N, se, 2), torch.float32)
+        GM = self._mask_spectrum(job.frames, job.mask_dev, H, P0, P1, C0, C1, pfx)
+        if half:
+            self.call("C_spectra", "zr_pack_half", GM.data_ptr(), 1, se, GM16.data_ptr(), hsc[2 * N:].data_ptr(),
+                      pw, 4 * N, st)
+        self._spectra_pass(job.frames, job.mask_dev, job.msub, N, H, P0, P1, C0, C1, G, S, pfx,
+                           half=(G16, S16, hsc, pw) if half else None)
+        spec = (half, G, S, GM, G16, S16, GM16, hsc)
+        if job.preshift:
+            job.pr, job.keep = self._preshift(reg, job.pairs, job.refine, N, C0, C1, job.pp, spec, st)
+        else:
+            job.pr = self._cropped_peaks(reg, job.pairs, job.refine, N, C0, C1, job.mS, job.pp, spec, st)
+            job.keep = np.ones(len(job.pairs), dtype=bool)
+
+    @staticmethod
+    def batch_key(job):
+        """Movies with equal keys share the launches of the batched path: the
+        same frame shape and pixel type, the same corrections, transform
+        sizes and peak search.  None: the movie goes alone (preShift,
+        triMode 'refine', half-precision spectra, a user mask)."""
+        if job.preshift or job.refine or job.half or job.user_mask:
+            return None
+        r = job.reg
+        pp = job.pp
+        return (job.H, job.W, job.rtype, job.gain is not None, job.ha is not None, job.gdiv, job.msub is not None,
+                job.P0, job.P1, job.C0, job.C1, job.mS, pp.bmode, pp.sub_pix_reg, pp.suppress_origin,
+                pp.conv_sigma_y, pp.conv_sigma_x, bool(r.subtractFrameMean))
+
+    def _correlate_batch(self, jobs, cls):
+        torch = self.torch
+        st = self.stream
+        j0 = jobs[0]
+        H, W, P0, P1, C0, C1, mS = j0.H, j0.W, j0.P0, j0.P1, j0.C0, j0.C1, j0.mS
+        w = 2 * mS
+        pfx = cls
+        Ns = [j.N for j in jobs]
+        offs = np.concatenate([[0], np.cumsum(Ns)]).astype(np.int64)
+        NT = int(offs[-1])
+        HW = H * W
+        # the movies' frames and maps side by side (device copies)
+        tdt = j0.raw.dtype
+        raw = self.tensor(pfx + "raw", (NT, H, W), tdt)
+        for j, f0 in zip(jobs, offs):
+            raw[int(f0):int(f0) + j.N].copy_(j.raw)
+
+        def stacked(name, attr):
+            if getattr(j0, attr) is None:
+                return None
+            t = self.tensor(pfx + name, (len(jobs), H, W), torch.float32)
+            for k, j in enumerate(jobs):
+                t[k].copy_(getattr(j, attr).reshape(H, W))
+            return t
+        gain, ha, hb = stacked("gain", "gain"), stacked("hot_a", "ha"), stacked("hot_b", "hb")
+        fmap = torch.from_numpy(np.repeat(np.arange(len(jobs), dtype=np.int32), Ns)).to(self.dev, non_blocking=True)
+        frames = Frames(raw.data_ptr(), j0.rtype, gain.data_ptr() if gain is not None else None,
+                        ha.data_ptr() if ha is not None else None, hb.data_ptr() if hb is not None else None,
+                        float(j0.gdiv), NT, H, W, HW, fmap.data_ptr(), HW)
+        msub = None
+        if j0.msub is not None:
+            msub = self.tensor(pfx + "msub", (NT,), torch.float64)
+            for j, f0 in zip(jobs, offs):
+                msub[int(f0):int(f0) + j.N].copy_(j.msub)
+        se = int(self.lib.zr_spectrum_elems(C0, C1))
+        G = self.tensor(pfx + "G", (NT, se, 2), torch.float32)
+        S = self.tensor(pfx + "S", (NT, se, 2), torch.float32)
+        GM = self._mask_spectrum(j0.frames, None, H, P0, P1, C0, C1, pfx)
+        self._spectra_pass(frames, None, msub, NT, H, P0, P1, C0, C1, G, S, pfx)
+        # frame terms of every frame, then every movie's pairs at its frames' offsets
+        terms = self.tensor(pfx + "terms", (4 * NT + 1, w, w), torch.float32)
+        pairs = np.concatenate([j.pairs + int(f0) for j, f0 in zip(jobs, offs)]).astype(np.int32)
+        M = len(pairs)
+        xw = min(XCORR_WORK, max(self.lib.zr_xcorr_work_bytes(1, C1, mS), self.lib.zr_xcorr_work_bytes(M, C1, mS)))
+        xptr = self.ptr(pfx + "xcwork", xw)
+        self.call("D_frame_terms", "zr_xcorr_terms", G.data_ptr(), S.data_ptr(), GM.data_ptr(), NT, C0, C1, mS,
+                  terms.data_ptr(), xptr, xw, st)
+        cwin = self.tensor(pfx + "cwin", (max(M, 1), w, w), torch.float32)
+        pairs_dev = torch.from_numpy(pairs.reshape(-1)).to(self.dev, non_blocking=True)
+        self.call("E_pairs", "zr_xcorr_pairs", G.data_ptr(), terms.data_ptr(), pairs_dev.data_ptr(), M, NT, C0, C1,
+                  mS, cwin.data_ptr(), xptr, xw, st)
+        pres = self.tensor(pfx + "peaks", (max(M, 1), C.sizeof(PeakResult)), torch.uint8)
+        self.call("F_peaks", "zr_locate_peaks", cwin.data_ptr(), M, mS, C.byref(j0.pp), pres.data_ptr(), st)
+        recs = np.frombuffer(pres[:M].cpu().numpy().tobytes(), dtype=_PEAK_DTYPE).copy()
+        k = 0
+        for j in jobs:
+            m = len(j.pairs)
+            j.pr = recs[k:k + m].copy()
+            j.keep = np.ones(m, dtype=bool)
+            k += m
+
+    # ------------------------------------------------------------------ solve, shifts, filters, FRC
+    def _finish(self, job):
+        """The drift solve, shifted sums, dose filter, FRC and outputs of one
+        movie."""
+        return self._finish_out(job, self._finish_main(job))
+
+    def _finish_main(self, job):
+        """The drift solve, the shifted sums and the dose filter of one movie
+        (zorro.py:1651-1712); keeps what the FRC and the outputs need on the
+        job and returns the outputs so far."""
+        torch = self.torch
+        st = self.stream
+        reg, pfx, bench = job.reg, job.pfx, job.bench
+        N, H, W, P0, P1, C0, C1 = job.N, job.H, job.W, job.P0, job.P1, job.C0, job.C1
+        pairs, pr, keep = job.pairs, job.pr, job.keep
+        filt, hotinfo, frames, pixelsize, user_mask = job.filt, job.hotinfo, job.frames, job.pixelsize, job.user_mask
+        refine = job.refine
         shifts = np.zeros([N, N, 2])
         corr = np.zeros([N, N])
         psig = np.zeros([N, N])
@@ -767,15 +1064,15 @@ class Engine:
         # integer roll only unless subPixReg > 1 with 'lanczos' (zorro.py:1790-1796)
         tab = hm.shift_table(translations, H, W, lanczos=reg.subPixReg > 1.0 and reg.shiftMethod == "lanczos")
         sh_dev = torch.from_numpy(tab.view(np.uint8)).to(self.dev, non_blocking=True)
-        isum = self.tensor("isum", (H, W), torch.float32)
+        isum = self.tensor(pfx + "isum", (H, W), torch.float32)
         # the even/odd half sums feed only the lazy FRC (the independent
         # even/odd FRC registers the halves again)
         lazy = bool(reg.doLazyFRC) and not reg.doEvenOddFRC
-        esum = self.tensor("esum", (H, W), torch.float32) if lazy else None
-        osum = self.tensor("osum", (H, W), torch.float32) if lazy else None
+        esum = self.tensor(pfx + "esum", (H, W), torch.float32) if lazy else None
+        osum = self.tensor(pfx + "osum", (H, W), torch.float32) if lazy else None
         need_aligned = (reg.keepAlignedImages or bool(reg.doEvenOddFRC) or
                         any(f in ("dose", "dosenorm") for f in filt))
-        aligned = self.tensor("aligned", (N, H, W), torch.float32) if need_aligned else None
+        aligned = self.tensor(pfx + "aligned", (N, H, W), torch.float32) if need_aligned else None
         self.call("G_shift_sum", "zr_shift_sum", C.byref(frames), sh_dev.data_ptr(), isum.data_ptr(),
                   esum.data_ptr() if lazy else None, osum.data_ptr() if lazy else None,
                   aligned.data_ptr() if aligned is not None else None, st)
@@ -801,16 +1098,32 @@ class Engine:
                 perf = self.lib.zr_dose_work_bytes(P0, P1, 1) - fixed
                 nch = max(2, min(N + (N & 1), (DOSE_WORK - fixed) // perf))
                 dwb = fixed + nch * perf
-                filt_sum = self.tensor("filtsum", (H, W), torch.float32)
+                filt_sum = self.tensor(pfx + "filtsum", (H, W), torch.float32)
                 self.call("I_dose", "zr_dose_filter", aligned.data_ptr(), N, H, W, C.byref(dp), tq.data_ptr(), de.data_ptr(),
-                          P0, P1, filt_sum.data_ptr(), self.ptr("dosework", dwb), dwb, st)
+                          P0, P1, filt_sum.data_ptr(), self.ptr(pfx + "dosework", dwb), dwb, st)
         bench["dose1"] = time.time()
 
+        job.translations, job.isum, job.esum, job.osum = translations, isum, esum, osum
+        job.aligned, job.aligned_ready, job.filt_sum = aligned, aligned_ready, filt_sum
+        return out
+
+    def _finish_out(self, job, out, halves=None):
+        """FRC (lazy, or the independent even/odd FRC) and the outputs of one
+        movie.  ``halves``: (FRC, FRC2D, transEven, transOdd, half-set error
+        dictionaries) when the batched path has registered the half sets."""
+        torch = self.torch
+        st = self.stream
+        reg, pfx, bench = job.reg, job.pfx, job.bench
+        H, W, N = job.H, job.W, job.N
+        hotinfo, filt, pixelsize, user_mask = job.hotinfo, job.filt, job.pixelsize, job.user_mask
+        translations, isum, esum, osum = job.translations, job.isum, job.esum, job.osum
+        aligned, filt_sum = job.aligned, job.filt_sum
         # ---- lazy FRC (zorro.py:2226-2310)
         frc = frc2d = None
         if reg.doEvenOddFRC:
-            frc, frc2d, out["transEven"], out["transOdd"], out["halfSetErrorDicts"] = self._even_odd_frc(
-                reg, aligned, hotinfo, filt, aligned_ready)
+            if halves is None:
+                halves = self._even_odd_frc(reg, aligned, hotinfo, filt, job.aligned_ready)
+            frc, frc2d, out["transEven"], out["transOdd"], out["halfSetErrorDicts"] = halves
         elif reg.doLazyFRC:
             offs, tiles = hm.frc_tiles((H, W), translations)
             box = 512
@@ -823,10 +1136,10 @@ class Engine:
                 offs_dev = torch.from_numpy(offs.reshape(-1)).to(self.dev, non_blocking=True)
                 nr = box // 2
                 fwb = self.lib.zr_frc_work_bytes(len(offs), box)
-                f2 = self.tensor("frc2d", (box, box), torch.float32)
-                fr = self.tensor("frc", (nr,), torch.float64)
+                f2 = self.tensor(pfx + "frc2d", (box, box), torch.float32)
+                fr = self.tensor(pfx + "frc", (nr,), torch.float64)
                 self.call("H_frc", "zr_tiled_frc", esum.data_ptr(), osum.data_ptr(), H, W, box, offs_dev.data_ptr(), len(offs),
-                          f2.data_ptr(), fr.data_ptr(), nr, self.ptr("frcwork", fwb), fwb, st)
+                          f2.data_ptr(), fr.data_ptr(), nr, self.ptr(pfx + "frcwork", fwb), fwb, st)
                 frc2d, frc = f2, fr
         bench["frc1"] = time.time()
 

@@ -20,7 +20,11 @@ detector software writes:
 host memory, so the copy to the GPU is one asynchronous transfer.  A mode-101
 movie is returned packed (``Packed4``): the packed bytes are what crosses the
 host link, and the GPU path expands them in HBM (``zr_unpack_u4``).
-Compressed files (.mrcz, .bz2, .gz) are not read.
+
+MRCZ files are MRC files whose mode word also names a compressor (mode +
+1000 x code: 1 blosclz, 2 lz4, 3 lz4hc, 4 snappy, 5 zlib, 6 zstd) and whose
+z-slices follow the header as one blosc chunk each (``blosc``); without a
+compressor an .mrcz file is a plain MRC file.  .bz2/.gz files are not read.
 """
 from __future__ import annotations
 
@@ -33,6 +37,7 @@ HEADER_BYTES = 1024
 IMOD_STAMP = 1146047817
 IMOD_SIGNED_BYTES = 1
 MODE_U4 = 101
+MRCZ_COMPRESSORS = {0: None, 1: "blosclz", 2: "lz4", 3: "lz4hc", 4: "snappy", 5: "zlib", 6: "zstd"}
 _MODE_DTYPES = {1: "i2", 2: "f4", 4: "c8", 6: "u2", 12: "f2"}
 _DTYPE_MODES = {"int8": 0, "uint8": 0, "int16": 1, "float32": 2, "complex64": 4, "uint16": 6, "float16": 12}
 
@@ -68,7 +73,7 @@ def _byteorder(raw):
     # no stamp (older writers): the order in which the mode word is sane
     for bo in ("<", ">"):
         mode = struct.unpack(bo + "i", raw[12:16])[0]
-        if mode in (0, 1, 2, 4, 6, 12, MODE_U4):
+        if mode >= 0 and mode % 1000 in (0, 1, 2, 4, 6, 12, MODE_U4) and mode // 1000 in MRCZ_COMPRESSORS:
             return bo
     raise ValueError("not an MRC file: unknown byte order and mode")
 
@@ -91,6 +96,14 @@ def parse_header(raw):
     nl = struct.unpack(bo + "i", raw[220:224])[0]
     h["labels"] = [raw[224 + 80 * i:304 + 80 * i].rstrip(b"\x00 ").decode("latin-1") for i in range(max(0, min(nl, 10)))]
     h["byteorder"] = bo
+    # MRCZ: the compressor in the thousands of the mode word
+    if h["mode"] >= 1000:
+        if h["mode"] // 1000 not in MRCZ_COMPRESSORS:
+            raise ValueError("MRC mode %d: unknown compressor code %d" % (h["mode"], h["mode"] // 1000))
+        h["compressor"] = MRCZ_COMPRESSORS[h["mode"] // 1000]
+        h["mode"] %= 1000
+    else:
+        h["compressor"] = None
     if h["nx"] <= 0 or h["ny"] <= 0 or h["nz"] <= 0:
         raise ValueError("MRC header with empty shape %s" % ((h["nx"], h["ny"], h["nz"]),))
     # Angstrom per pixel along x, y, z (0 where the sampling is unset)
@@ -132,16 +145,20 @@ def read(path, pinned=False):
     own type (native byte order), or a ``Packed4`` for mode 101.  With
     ``pinned`` the data live in page-locked host memory."""
     ext = os.path.splitext(str(path))[1].lower()
-    if ext in (".mrcz", ".mrczs", ".mrcsz", ".bz2", ".gz", ".7z"):
-        raise ValueError("compressed MRC files (%s) are not read: decompress first" % ext)
+    if ext in (".bz2", ".gz", ".7z"):
+        raise ValueError("compressed files (%s) are not read: decompress first" % ext)
     with open(path, "rb") as fh:
         h = parse_header(fh.read(HEADER_BYTES))
         fh.seek(HEADER_BYTES + max(0, h["nsymbt"]))
         nz, ny, nx = h["nz"], h["ny"], h["nx"]
         dt = data_dtype(h)
-        nbytes = nz * ny * ((nx + 1) // 2) if dt is None else nz * ny * nx * dt.itemsize
+        slice_bytes = ny * ((nx + 1) // 2) if dt is None else ny * nx * dt.itemsize
+        nbytes = nz * slice_bytes
         buf = _host_buffer(nbytes, pinned)
-        got = fh.readinto(memoryview(buf))
+        if h["compressor"] is None:
+            got = fh.readinto(memoryview(buf))
+        else:
+            got = _read_blosc_slices(fh, nz, slice_bytes, buf)
     if got != nbytes:
         raise ValueError("MRC data truncated: %d of %d bytes" % (got, nbytes))
     if dt is None:
@@ -150,6 +167,25 @@ def read(path, pinned=False):
     if dt.byteorder == ">":
         a = a.byteswap(inplace=True).view(dt.newbyteorder("="))
     return a, h
+
+
+def _read_blosc_slices(fh, nz, slice_bytes, buf):
+    """MRCZ data: one blosc chunk per z-slice, each as long as its header
+    says; decoded into ``buf``.  Returns the bytes decoded."""
+    from . import blosc
+    got = 0
+    for z in range(nz):
+        head = fh.read(blosc.HEADER)
+        if len(head) < blosc.HEADER:
+            break
+        cbytes = blosc.chunk_header(head)[6]
+        chunk = head + fh.read(cbytes - blosc.HEADER)
+        data = blosc.decompress(chunk)
+        if len(data) != slice_bytes:
+            raise ValueError("MRCZ slice %d holds %d bytes, not %d" % (z, len(data), slice_bytes))
+        buf[z * slice_bytes:(z + 1) * slice_bytes] = np.frombuffer(data, dtype=np.uint8)
+        got += len(data)
+    return got
 
 
 def _stats(a):

@@ -182,7 +182,9 @@ class ImageRegistrator:
           (``loadGainRef``); 'sum'/'imageSum', 'filt'/'filtSum' and 'mask'
           set those attributes.
 
-        DM3/DM4/TIFF/HDF5 and compressed files are not read."""
+        DM4 files (``dm4.read``) give their second image and its calibration,
+        voltage and Cs; MRCZ files are read by ``mrc.read`` (blosc-compressed
+        slices).  DM3/TIFF/HDF5 and .bz2/.gz files are not read."""
         import os
 
         from . import mrc
@@ -192,11 +194,26 @@ class ImageRegistrator:
         if not name:
             raise ValueError("zorro.loadData: no file for target %r" % target)
         ext = os.path.splitext(str(name))[1].lower()
-        if ext not in (".mrc", ".mrcs"):
-            raise ValueError("zorro.loadData: %s files are not supported (MRC .mrc/.mrcs only)" % ext)
-        data, hdr = mrc.read(name, pinned=target in ("stack", "align", "images"))
-        if not np.isclose(hdr["pixelsize"][0], 0.0):
-            self.pixelsize = np.float32(hdr["pixelsize"][0])
+        if ext == ".dm4":
+            # zorro.py:3384-3411: the second image of the file (the first is
+            # the thumbnail), its calibration (nm) unless it has no units, the
+            # microscope's voltage (kV) and Cs
+            from . import dm4
+            data, info = dm4.read(name)
+            if data.ndim == 2:
+                data = data[None]
+            if info["pixelsize"] is not None:
+                self.pixelsize = info["pixelsize"]
+            if info["voltage"]:
+                self.voltage = info["voltage"]
+            if info["C3"]:
+                self.C3 = info["C3"]
+        elif ext in (".mrc", ".mrcs", ".mrcz", ".mrczs"):
+            data, hdr = mrc.read(name, pinned=target in ("stack", "align", "images"))
+            if not np.isclose(hdr["pixelsize"][0], 0.0):
+                self.pixelsize = np.float32(hdr["pixelsize"][0])
+        else:
+            raise ValueError("zorro.loadData: %s files are not supported (MRC, MRCZ or DM4)" % ext)
         if target in ("stack", "align", "images"):
             if data.ndim != 3 or data.shape[0] < 2:  # a single image, saved by mistake
                 self.METAstatus = "error"
@@ -274,6 +291,25 @@ class ImageRegistrator:
             raise ValueError("Zorro.alignImageStack: only xcorrMode 'zorro' runs on the GPU, not %s" % self.xcorrMode)
         from .engine import Engine
         Engine.get(self.device).align(self)
+
+
+def alignImageStacks(registrators, device=None):
+    """Register several movies at once on one GPU: alignImageStack for each
+    registrator (each keeps its own settings, detector size and frame count),
+    with the transform-heavy stages of movies that share a shape class run
+    as one set of launches (Engine.align_batch).  The outputs are those each
+    registrator gets from alignImageStack alone.  Has no counterpart in the
+    reference, which registers one movie per process."""
+    regs = list(registrators)
+    if not regs:
+        return regs
+    for r in regs:
+        if str(r.xcorrMode).lower() != "zorro":
+            raise ValueError("Zorro.alignImageStack: only xcorrMode 'zorro' runs on the GPU, not %s" % r.xcorrMode)
+    from .engine import Engine
+    dev = regs[0].device if device is None else device
+    Engine.get(dev).align_batch(regs)
+    return regs
 
 
 def copy_config(src, dst):

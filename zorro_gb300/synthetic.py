@@ -13,14 +13,22 @@ random-phase specimen, a drift trajectory, Poisson counting noise.
   plus i.i.d. ``N(0, jitter)`` jitter, centroid-zeroed.  Frame ``j`` is the
   specimen Fourier-shifted by ``drift[j]`` (exact sub-pixel), then cropped.
 * Counts: ``Poisson(mean_dose * frame / gain)``.  With ``dtype='uint8'`` the
-  counts are stored as bytes (clipped at 255); a multiplicative gain map
-  ``U(0.9, 1.1)`` and a fraction of hot pixels at ``hot_factor * mean_dose``
-  counts are added when asked.
+  counts are stored as bytes (clipped at 255), with ``'float16'`` as half
+  floats (exact up to 2048); a multiplicative gain map ``U(0.9, 1.1)`` and a
+  fraction of hot pixels at ``hot_factor * mean_dose`` counts are added when
+  asked.
+
+Every frame draws from its own random stream (spawned from ``seed``) and
+transforms with the same FFT thread count, so frames are generated in
+parallel threads (``workers``) with the same result for any thread count.
 
 ``images`` is what ``ImageRegistrator.alignImageStack`` receives after the
 reference's ``loadData`` applies the gain: ``float32(gain * raw)``.
 """
 from __future__ import annotations
+
+import concurrent.futures
+import os
 
 import numpy as np
 import scipy.fft
@@ -49,10 +57,10 @@ def drift_trajectory(rng, n_frames, drift_sigma, jitter=0.1):
 
 def make_movie(n_frames, shape, *, seed, mean_dose=1.0, drift_sigma=0.8, jitter=0.1,
                lowpass=1.0 / 8.0, contrast=0.1, dtype="float32", gain_map=False,
-               hot_fraction=0.0, hot_factor=50.0):
+               hot_fraction=0.0, hot_factor=50.0, workers=None, with_images=True):
     """Return a dict with ``raw`` (counts), ``gain`` (or None), ``images``
-    (float32 gain-corrected frames), ``drift`` ([N,2] y,x truth) and ``hot``
-    (flat indices of planted hot pixels)."""
+    (float32 gain-corrected frames; None without ``with_images``), ``drift``
+    ([N,2] y,x truth) and ``hot`` (flat indices of planted hot pixels)."""
     H, W = int(shape[0]), int(shape[1])
     rng = np.random.Generator(np.random.PCG64(seed))
     drift = drift_trajectory(rng, n_frames, drift_sigma, jitter)
@@ -64,15 +72,19 @@ def make_movie(n_frames, shape, *, seed, mean_dose=1.0, drift_sigma=0.8, jitter=
     fy = np.fft.fftfreq(cy).astype(np.float64)
     fx = np.fft.rfftfreq(cx).astype(np.float64)
     gain = rng.uniform(0.9, 1.1, size=(H, W)).astype(np.float32) if gain_map else None
-    raw_dtype = np.uint8 if dtype == "uint8" else np.float32
+    raw_dtype = {"uint8": np.uint8, "float16": np.float16}.get(dtype, np.float32)
     raw = np.empty((n_frames, H, W), dtype=raw_dtype)
     n_hot = int(round(hot_fraction * H * W))
     hot = np.sort(rng.choice(H * W, size=n_hot, replace=False)) if n_hot else np.zeros(0, dtype=np.int64)
     frame_rngs = [np.random.Generator(np.random.PCG64(s)) for s in
                   np.random.SeedSequence(seed).spawn(n_frames)]
-    for j in range(n_frames):
+
+    def one(j):
         dy, dx = drift[j]
         ramp = (np.exp(-2j * np.pi * fy * dy)[:, None] * np.exp(-2j * np.pi * fx * dx)[None, :]).astype(np.complex64)
+        # every call with all cores: the split of rows between FFT threads
+        # changes the last bits on some platforms, so it must not depend on
+        # how many frames are in flight
         frame = scipy.fft.irfft2(S * ramp, s=(cy, cx), workers=-1)[pad:pad + H, pad:pad + W]
         lam = np.clip(mean_dose * frame, 0.0, None)
         if gain is not None:
@@ -84,7 +96,17 @@ def make_movie(n_frames, shape, *, seed, mean_dose=1.0, drift_sigma=0.8, jitter=
         if n_hot:
             counts.reshape(-1)[hot] = raw_dtype(round(hot_factor * mean_dose))
         raw[j] = counts
-    if gain is not None:
+
+    nw = max(1, min(n_frames, workers if workers is not None else (1 if H * W < (1 << 22) else (os.cpu_count() or 1))))
+    if nw == 1:
+        for j in range(n_frames):
+            one(j)
+    else:
+        with concurrent.futures.ThreadPoolExecutor(nw) as ex:
+            list(ex.map(one, range(n_frames)))
+    if not with_images:
+        images = None
+    elif gain is not None:
         images = (gain[None, :, :] * raw.astype(np.float32)).astype(np.float32)
     else:
         images = raw.astype(np.float32)

@@ -17,8 +17,18 @@ and drift of the configuration it stands for.
 * ``k2x10`` -- the K2 movie cut to 10 frames (142 MB of counts, still larger
   than L2).
 * ``small`` -- ``config1`` without the even/odd FRC.
+
+``CONFIG4`` is the batched uneven workload: 16 movies of three detector
+shapes in the proportions 8 / 5 / 3 -- K2 counting movies (40 x 3838 x 3710
+uint8, mean 0.8, gain map and hot pixels), 4096 x 4096 float16 movies (30
+frames, mean 1.5) and K3 super-resolution movies (50 x 8184 x 11520 uint8,
+mean 0.25) Fourier-binned 2x to 4092 x 5760, each shape with its own drift
+random-walk step drawn from U(0.5, 2.0) px/frame; full triangles, maxShift
+100, dose filter, lazy FRC.
 """
 from __future__ import annotations
+
+import numpy as np
 
 K2_DOSE = [1.2 * 1.05 ** 2, 0.24499, -1.6649, 2.8141, 32, 0]
 CONFIG1_DOSE = [1.0, 0.24499, -1.6649, 2.8141, 32, 0]
@@ -45,3 +55,44 @@ def workload(name):
     """(movie kwargs, attrs) of a named workload, as fresh copies."""
     wl = WORKLOADS[name]
     return dict(wl["movie"]), dict(wl["attrs"])
+
+
+CONFIG4 = {
+    "k2": dict(count=8, movie=dict(n_frames=40, shape=(3838, 3710), mean_dose=0.8, dtype="uint8", gain_map=True,
+                                   hot_fraction=1e-4, hot_factor=50.0),
+               attrs=dict(triMode="tri", shapePadded=[4096, 4096], fouCrop=[2048, 2048], maxShift=100,
+                          pixelsize=0.105, voltage=300.0, filterMode="hot,dose", doseFiltParam=K2_DOSE, subPixReg=16)),
+    "f16": dict(count=5, movie=dict(n_frames=30, shape=(4096, 4096), mean_dose=1.5, dtype="float16"),
+                attrs=dict(triMode="tri", shapePadded=[4096, 4096], fouCrop=[2048, 2048], maxShift=100,
+                           pixelsize=0.1, voltage=300.0, filterMode="dose", doseFiltParam=CONFIG1_DOSE, subPixReg=16)),
+    "superres": dict(count=3, movie=dict(n_frames=50, shape=(8184, 11520), mean_dose=0.25, dtype="uint8"),
+                     attrs=dict(triMode="tri", shapeBinned=[4092, 5760], shapePadded=[4096, 6144],
+                                fouCrop=[2048, 3072], maxShift=100, pixelsize=0.0525, voltage=300.0,
+                                filterMode="dose", doseFiltParam=CONFIG1_DOSE, subPixReg=16)),
+}
+
+
+def config4_movies(seed=404, with_images=False, n_frames=None):
+    """One seeded movie of each CONFIG4 shape (drift step from U(0.5, 2.0))
+    and the shapes' settings: {shape: (movie dict, attrs, count)}.  With
+    ``n_frames`` every movie gets that many frames (a movie's first n frames
+    are then a movie of n frames: the served workload draws its frame counts
+    that way)."""
+    from .synthetic import make_movie
+    rng = np.random.default_rng(seed)
+    out = {}
+    for k, (name, spec) in enumerate(CONFIG4.items()):
+        sigma = float(rng.uniform(0.5, 2.0))
+        mk = dict(spec["movie"], seed=seed + k, drift_sigma=sigma)
+        if n_frames is not None:
+            mk["n_frames"] = int(n_frames)
+        mv = make_movie(**mk, with_images=with_images)
+        out[name] = (mv, dict(spec["attrs"]), spec["count"])
+    return out
+
+
+# The served workload: Poisson arrivals at each rate, shapes drawn 50/30/20
+# from CONFIG4's three, frame counts uniform in [20, 60], 160 GB of device
+# memory for the movies in flight.
+CONFIG5 = {"rates": (0.5, 1.0, 2.0, 4.0), "mix": {"k2": 0.5, "f16": 0.3, "superres": 0.2},
+           "frames": (20, 60), "hbm_budget": 160e9}
