@@ -354,6 +354,45 @@ int zr_dose_filter(const float* aligned, int N, int H, int W, const zr_dose_para
                    const float* thres_q, const float* dose_end, int P0, int P1, float* filt_sum,
                    void* work, size_t work_bytes, void* stream);
 
+/* ---- batches of movies: ImageRegistrator.alignImageStack over several
+ * movies of one shape (zorro.py:773-1231 per movie) ----
+ * A context holds the device buffers of the correlation stages for one shape
+ * class (frame size, padded and cropped sizes, maxShift), sized by the limits
+ * when it is created; zr_ctx_create is the one entry point here that
+ * allocates.  zr_submit_batch queues, on ``stream``, the forward spectra of
+ * every frame of every movie (xcorrnm2_tri, zorro.py:875-914), the frame
+ * terms and the pair windows (mnxc2, zorro.py:1014-1097) and the peak search
+ * (locatePeak, zorro.py:1099-1231) as one set of launches over all movies,
+ * and returns.  zr_poll returns 1 when the batch has finished (0 while it
+ * runs, a negative code on a CUDA error) and then has copied each movie's
+ * records to its ``peaks`` (n_pairs records, in the order of its pairs);
+ * zr_wait blocks until then.  One batch is in flight per context.  Every
+ * record equals what the per-stage entry points give for that movie alone.
+ * The drift solve and the later stages (zr_logistic_fit, zr_l1_solve,
+ * zr_shift_sum, zr_dose_filter, zr_tiled_frc) follow per movie. */
+typedef struct zr_ctx zr_ctx_t;
+typedef struct zr_batch_limits {
+  int height, width;      /* frame size (every movie of the class) */
+  int P0, P1, C0, C1;     /* padded and Fourier-cropped sizes */
+  int max_shift;          /* maxShift */
+  int max_frames;         /* frames of all movies of one batch, at most */
+  int max_pairs;          /* pairs of all movies of one batch, at most */
+  int chunk_frames;       /* frames transformed per spectra launch */
+} zr_batch_limits_t;
+typedef struct zr_batch_movie {
+  zr_frames_t frames;       /* the movie's frames (device); frame_movie NULL */
+  const double* mean_sub;   /* [n_frames] subtracted before the transform (device; NULL: 0) */
+  const int* pairs;         /* [n_pairs][2] (I, J), host memory, read during the call */
+  int n_pairs;
+  zr_peak_result_t* peaks;  /* [n_pairs] host memory, written by zr_poll / zr_wait */
+} zr_batch_movie_t;
+int zr_ctx_create(int device, const zr_batch_limits_t* limits, zr_ctx_t** ctx);
+int zr_ctx_destroy(zr_ctx_t* ctx);
+int zr_submit_batch(zr_ctx_t* ctx, const zr_batch_movie_t* movies, int n_movies, const zr_peak_params_t* params,
+                    void* stream);
+int zr_poll(zr_ctx_t* ctx);
+int zr_wait(zr_ctx_t* ctx);
+
 /* ---- compressed movie files: MRCZ (zorro.loadData, zorro.py:3414) ---- */
 
 /* Decode one LZ4 block (blosc's LZ4 and LZ4HC codecs) of src_bytes into

@@ -304,7 +304,8 @@ def test_struct_layouts_match_the_header(tmp_path):
         pytest.skip("no C compiler")
     pairs = {"zr_frames_t": _lib.Frames, "zr_hotpix_params_t": _lib.HotpixParams, "zr_peak_params_t": _lib.PeakParams,
              "zr_peak_result_t": _lib.PeakResult, "zr_shift_t": _lib.Shift, "zr_dose_params_t": _lib.DoseParams,
-             "zr_plan_shape_t": _lib.PlanShape, "zr_plan_choice_t": _lib.PlanChoice}
+             "zr_plan_shape_t": _lib.PlanShape, "zr_plan_choice_t": _lib.PlanChoice,
+             "zr_batch_limits_t": _lib.BatchLimits, "zr_batch_movie_t": _lib.BatchMovie}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "zorro_gb300.h"', "int main(void) {"]
     for cname, cls in pairs.items():
         lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))

@@ -19,6 +19,7 @@ from zorro_gb300.synthetic import make_movie
 pytestmark = pytest.mark.gpu
 
 DOSE = [1.0, 0.24499, -1.6649, 2.8141, 32, 0]
+ZR_EINVAL, ZR_ESIZE = -1, -3
 
 
 def make_reg(images, gain=None, **attrs):
@@ -124,3 +125,90 @@ def test_superres_movie_binned_and_registered_against_oracle():
     assert np.mean(d < 1e-9) >= 0.9
     assert np.abs(reg.translations - t).max() <= 1e-6
     assert rel <= 1e-4
+
+
+def _tri(n):
+    return [(i, j) for i in range(n) for j in range(i + 1, n)]
+
+
+def test_batch_context_records_equal_each_movie_alone():
+    """zr_ctx_create / zr_submit_batch / zr_poll / zr_wait: three movies of
+    one shape (6, 9 and 5 frames) in one batch give, record for record and
+    bit for bit, the peaks of each movie's own per-stage calls; a second
+    batch on the same context in another order gives them again, and
+    batches beyond the context's limits are refused before anything runs."""
+    import ctypes as C
+    import time
+
+    import torch
+
+    from tests import gpu_helpers as gh
+    from zorro_gb300 import _lib
+    P, C_, mS = (256, 256), (128, 128), 16
+    movies = [make_movie(n, (200, 190), seed=70 + n, mean_dose=2.0, drift_sigma=1.0)["images"] for n in (6, 9, 5)]
+    alone = []
+    for imgs in movies:
+        _, _, _, _, dev = gh.spectra(imgs, P, C_)
+        _, _, cwin = gh.windows(dev, imgs.shape[0], C_, mS, _tri(imgs.shape[0]))
+        alone.append(gh.peaks(cwin, mS))
+
+    lib = _lib.load()
+    dev = torch.cuda.current_device()
+    lim = _lib.BatchLimits(200, 190, P[0], P[1], C_[0], C_[1], mS, 20, 60, 4)
+    ctx = C.c_void_p()
+    _lib.call("zr_ctx_create", dev, C.byref(lim), C.byref(ctx))
+    pp = _lib.PeakParams()
+    pp.sub_pix_reg, pp.bmode, pp.suppress_origin, pp.use_mask = 16, 1, 1, 1
+    pp.opti_lo, pp.opti_hi, pp.opti_xatol, pp.opti_maxiter = 0.0, 7.0, 0.01, 15
+    try:
+        raws = [gh.dev_tensor(m.astype(np.float32)) for m in movies]
+        msubs = []
+        for r in raws:
+            ms = torch.zeros(r.shape[0], dtype=torch.float64, device="cuda")
+            _lib.call("zr_frame_sums", C.byref(gh.frames_of(r)), ms.data_ptr(), gh.stream())
+            msubs.append(ms)
+
+        def run(order):
+            pairs = [np.asarray(_tri(movies[k].shape[0]), dtype=np.int32).reshape(-1) for k in order]
+            outs = [np.zeros(len(p) // 2, dtype=gh.PEAK_DTYPE) for p in pairs]
+            arr = (_lib.BatchMovie * len(order))()
+            for slot, k in enumerate(order):
+                arr[slot] = _lib.BatchMovie(gh.frames_of(raws[k]), msubs[k].data_ptr(), pairs[slot].ctypes.data,
+                                            len(pairs[slot]) // 2, outs[slot].ctypes.data)
+            _lib.call("zr_submit_batch", ctx, arr, len(order), C.byref(pp), gh.stream())
+            t0 = time.time()
+            while True:
+                done = lib.zr_poll(ctx)
+                assert done >= 0, _lib.last_error()
+                if done == 1 or time.time() - t0 > 60:
+                    break
+                time.sleep(0.001)
+            _lib.call("zr_wait", ctx)
+            assert lib.zr_poll(ctx) == 1
+            return {k: outs[slot] for slot, k in enumerate(order)}
+
+        for order in ((0, 1, 2), (2, 0, 1)):
+            got = run(order)
+            for k in range(3):
+                assert got[k].tobytes() == alone[k].tobytes(), (order, k)
+
+        # refused on the host: more frames than the context holds, a pair
+        # outside its movie, a frame size of another class
+        big = (_lib.BatchMovie * 3)()
+        p9 = np.asarray(_tri(9), dtype=np.int32).reshape(-1)
+        out9 = np.zeros(len(p9) // 2, dtype=gh.PEAK_DTYPE)
+        for s in range(3):
+            big[s] = _lib.BatchMovie(gh.frames_of(raws[1]), None, p9.ctypes.data, len(p9) // 2, out9.ctypes.data)
+        assert lib.zr_submit_batch(ctx, big, 3, C.byref(pp), gh.stream()) == ZR_ESIZE
+        bad = np.asarray([0, 9], dtype=np.int32)
+        one = (_lib.BatchMovie * 1)(_lib.BatchMovie(gh.frames_of(raws[1]), None, bad.ctypes.data, 1,
+                                                    out9.ctypes.data))
+        assert lib.zr_submit_batch(ctx, one, 1, C.byref(pp), gh.stream()) == ZR_EINVAL
+        other = gh.dev_tensor(np.zeros((4, 100, 90), np.float32))
+        p4 = np.asarray(_tri(4), dtype=np.int32).reshape(-1)
+        one = (_lib.BatchMovie * 1)(_lib.BatchMovie(gh.frames_of(other), None, p4.ctypes.data, len(p4) // 2,
+                                                    out9.ctypes.data))
+        assert lib.zr_submit_batch(ctx, one, 1, C.byref(pp), gh.stream()) == ZR_ESIZE
+        torch.cuda.synchronize()
+    finally:
+        _lib.call("zr_ctx_destroy", ctx)

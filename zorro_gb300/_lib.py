@@ -24,6 +24,7 @@ EXPORTS = (
     "zr_xcorr_refine", "zr_pack_half", "zr_xcorr_terms_half", "zr_xcorr_pairs_half", "zr_bin_work_bytes",
     "zr_bin_fourier", "zr_unpack_u4", "zr_full_prepare", "zr_full_work_bytes", "zr_full_filter", "zr_full_peaks",
     "zr_plan_work_bytes", "zr_plan", "zr_plan_set", "zr_plan_get", "zr_lz4_decompress",
+    "zr_ctx_create", "zr_ctx_destroy", "zr_submit_batch", "zr_poll", "zr_wait",
 )
 
 
@@ -62,6 +63,21 @@ class PlanShape(C.Structure):
 class PlanChoice(C.Structure):
     _fields_ = [("fwd_rows", C.c_int), ("fwd_cols", C.c_int), ("xc_cols", C.c_int), ("xc_rows", C.c_int),
                 ("ms_spectra", (C.c_float * 3) * 3), ("ms_pairs", (C.c_float * 3) * 3)]
+
+
+class BatchLimits(C.Structure):
+    """zr_batch_limits_t: one shape class and the most frames and pairs of a
+    batch."""
+    _fields_ = [("height", C.c_int), ("width", C.c_int), ("P0", C.c_int), ("P1", C.c_int), ("C0", C.c_int),
+                ("C1", C.c_int), ("max_shift", C.c_int), ("max_frames", C.c_int), ("max_pairs", C.c_int),
+                ("chunk_frames", C.c_int)]
+
+
+class BatchMovie(C.Structure):
+    """zr_batch_movie_t: one movie of a batch (pairs and peaks in host
+    memory)."""
+    _fields_ = [("frames", Frames), ("mean_sub", C.c_void_p), ("pairs", C.c_void_p), ("n_pairs", C.c_int),
+                ("peaks", C.c_void_p)]
 
 
 class Shift(C.Structure):
@@ -136,6 +152,11 @@ _SIGS = {
     "zr_plan_set": (C.c_int, [C.POINTER(PlanShape), C.POINTER(PlanChoice)]),
     "zr_plan_get": (C.c_int, [C.POINTER(PlanShape), C.POINTER(PlanChoice)]),
     "zr_lz4_decompress": (C.c_longlong, [_P, C.c_size_t, _P, C.c_size_t]),
+    "zr_ctx_create": (C.c_int, [C.c_int, C.POINTER(BatchLimits), C.POINTER(C.c_void_p)]),
+    "zr_ctx_destroy": (C.c_int, [_P]),
+    "zr_submit_batch": (C.c_int, [_P, _P, C.c_int, C.POINTER(PeakParams), _P]),
+    "zr_poll": (C.c_int, [_P]),
+    "zr_wait": (C.c_int, [_P]),
 }
 
 

@@ -28,7 +28,7 @@ constexpr int DS_NBR = ZR_DS_NBR;
 // transforms, whose four-row tiles would not fit the register file
 __host__ __device__ constexpr int ds_nbr(int L) { return L > 4096 ? 2 : DS_NBR; }
 // CTAs per SM to ask the register allocator for: 128 registers a thread
-constexpr int ds_minb(int T) { return T >= 512 ? 1 : 512 / T; }
+constexpr int ds_minb(int T) { return sm_minb(T); }
 
 
 __device__ __forceinline__ int sym_idx(int i, int n) {

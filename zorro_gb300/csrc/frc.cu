@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(fft_threads(B, FRC_NB), fft_minblocks(B))
 }
 
 // CTAs per SM that keep a T-thread CTA at <= 128 registers per thread
-constexpr int frc_minblocks(int T) { return T >= 512 ? 1 : 512 / T; }
+constexpr int frc_minblocks(int T) { return sm_minb(T); }
 
 template <int B>
 __global__ void __launch_bounds__(fft_threads(B, 2 * FRC_NB), frc_minblocks(fft_threads(B, 2 * FRC_NB)))

@@ -39,6 +39,12 @@ constexpr int fft_threads(int L, int NB, int ept = ZR_FFT_EPT) {
 }
 // Resident CTAs per SM to ask the register allocator for (short transforms).
 constexpr int fft_minblocks(int L) { return L <= 2048 ? ZR_FFT_MINB : 1; }
+// CTAs of T threads per SM to ask the register allocator for, so that
+// ZR_SM_THREADS threads fit an SM (512: up to 128 registers a thread).
+#ifndef ZR_SM_THREADS
+#define ZR_SM_THREADS 512
+#endif
+__host__ __device__ constexpr int sm_minb(int T) { return T >= ZR_SM_THREADS ? 1 : ZR_SM_THREADS / T; }
 
 // Launch variants of the transform kernels, chosen per transform length by
 // the planner (zr_plan) or set from saved choices (zr_plan_set): sequences

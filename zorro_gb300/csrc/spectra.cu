@@ -22,7 +22,7 @@ constexpr int NBR = 4;  // rows per group of the row-pass output layout
 // 1, 2 or 4 per transform length (tune_get)
 constexpr int FR_DEFAULT = 2, FC_DEFAULT = 2;
 // CTAs per SM to ask the register allocator for: 128 registers a thread
-constexpr int minb_of(int T) { return T >= 512 ? 1 : 512 / T; }
+constexpr int minb_of(int T) { return sm_minb(T); }
 
 template <int P1, int FR>
 __global__ void __launch_bounds__(fft_threads(P1, FR), minb_of(fft_threads(P1, FR)))

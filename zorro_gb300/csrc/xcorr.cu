@@ -45,7 +45,7 @@ __host__ __device__ constexpr int xc_threads(int C0, int NBC) { return fft_threa
 #endif
 constexpr int XC_NBR_DEFAULT = 2;
 __host__ __device__ constexpr int xr_threads(int C1, int NBR) { return fft_threads(C1, NBR, ZR_XR_EPT); }
-__host__ __device__ constexpr int xr_minb(int T) { return T >= 512 ? 1 : 512 / T; }
+__host__ __device__ constexpr int xr_minb(int T) { return sm_minb(T); }
 
 struct XcJobs {
   const void* G;     // spectra: float2, or __half2 when ``sc`` is set
