@@ -720,6 +720,7 @@ def main():
     launches = lib.zr_launch_count() - launches0
     dev_ms = ev0.elapsed_time(ev1)
     stage_ms = eng.stage_ms()
+    host_ms = eng.host_ms()
     eng.profile = None
     if args.profile_only:
         return
@@ -869,7 +870,8 @@ def main():
             "movie_algorithmic_bytes": sum(ab.values()),
             "movie_frac": round(sum(ab.values()) / t_step / 1e9 / peak, 4),
             "fft_tflops": {k: round(v / (per_step[k] / 1000.0) / 1e12, 2) for k, v in fl.items() if k in per_step},
-            "fp32_peak_tflops": round(fp32_peak, 1)}
+            "fp32_peak_tflops": round(fp32_peak, 1),
+            "host_ms_per_step": {k: round(v / args.steps, 3) for k, v in sorted(host_ms.items())}}
 
     # ---- accuracy of the last timed movie (outside the timed region): against
     # the known drift, and against the float64 oracle's outputs for this

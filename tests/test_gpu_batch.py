@@ -99,7 +99,10 @@ def test_superres_movie_binned_and_registered_against_oracle():
     (Ten pairs leave the logistic weight fit a single histogram bin, an
     ill-posed fit whose optimum moves with the last digits of the peak
     significances, so the trajectory is checked through the solve rather
-    than against the oracle's own.)"""
+    than against the oracle's own; and ten weighted equations in five
+    unknowns can leave the weighted-L1 optimum a face rather than a vertex,
+    so the host solve is held to the oracle's weights and objective value,
+    not to the oracle solver's point of the face.)"""
     from zorro_gb300.registrator import alignImageStacks
     mv = make_movie(5, (8184, 11520), seed=61, mean_dose=1.0, drift_sigma=2.0, dtype="uint8")
     attrs = dict(triMode="tri", shapeBinned=[4092, 5760], shapePadded=[4096, 6144], fouCrop=[2048, 3072],
@@ -117,13 +120,21 @@ def test_superres_movie_binned_and_registered_against_oracle():
     d = np.abs(ed["shiftsTriMat"] - ref["errorDict"]["shiftsTriMat"]).max(axis=2)[tri]
     o = zo.shifts_solver(ed["shiftsTriMat"], ed["corrTriMat"], ed["peaksigTriMat"], shapeImage=attrs["shapePadded"],
                          maxShift=attrs["maxShift"])
-    t = o["translations"] - o["translations"].mean(axis=0)
+    np.testing.assert_allclose(ed["weights"], o["weights"], rtol=1e-12)
+    used = ed["corrTriMat"][:-1, 1:].astype(bool)
+    A = zo.solver_matrix(used)
+    f = []
+    for ax in (0, 1):
+        b = ed["shiftsTriMat"][:-1, 1:, ax][used]
+        f.append((float(np.sum(o["weights"] * np.abs(A @ ed["relativeEst"][:, ax] - b))),
+                  float(np.sum(o["weights"] * np.abs(A @ o["relativeEst"][:, ax] - b)))))
     _, isum = zo.apply_shifts(binned.astype(np.float32), reg.translations, originMode=None)
     rel = np.linalg.norm(np.asarray(reg.imageSum, np.float64) - isum) / np.linalg.norm(isum)
-    print("super-res: %d pairs, %d exact; solve of the GPU measurements %.2e px; imageSum rel L2 %.2e" % (
-        tri.sum(), int(np.sum(d < 1e-9)), np.abs(reg.translations - t).max(), rel))
+    print("super-res: %d pairs, %d exact; L1 objectives (GPU, oracle) %s; imageSum rel L2 %.2e" % (
+        tri.sum(), int(np.sum(d < 1e-9)), f, rel))
     assert np.mean(d < 1e-9) >= 0.9
-    assert np.abs(reg.translations - t).max() <= 1e-6
+    for f_gpu, f_ora in f:
+        assert abs(f_gpu - f_ora) <= 1e-9 * max(1.0, f_ora)
     assert rel <= 1e-4
 
 

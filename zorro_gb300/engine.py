@@ -112,7 +112,18 @@ class Engine:
     def stage_ms(self):
         """Summed device time per stage of the recorded calls (synchronises)."""
         self.torch.cuda.synchronize(self.dev)
-        return {k: sum(a.elapsed_time(b) for a, b in v) for k, v in (self.profile or {}).items()}
+        return {k: sum(a.elapsed_time(b) for a, b in v) for k, v in (self.profile or {}).items()
+                if not k.startswith("host:")}
+
+    def host_ms(self):
+        """Summed host time of the host steps (CDF fits, drift solves) while
+        profiling was on."""
+        return {k[5:]: 1e3 * sum(v) for k, v in (self.profile or {}).items() if k.startswith("host:")}
+
+    def _host_time(self, step, t0):
+        if self.profile is not None:
+            with self._profile_lock:
+                self.profile.setdefault("host:" + step, []).append(time.perf_counter() - t0)
 
     # ------------------------------------------------------------------ planning
     def plan(self, P0, P1, C0, C1, mS, effort="FFTW_MEASURE", cache_dir=None):
@@ -717,7 +728,9 @@ class Engine:
             hist.zero_()
             self.call("A_gain_sum", "zr_histogram", usum.data_ptr(), H * W, float(edges[0]), nb, hist.data_ptr(), st)
             h = hist[:nb].cpu().numpy().astype(np.int64)
+            t_fit = time.perf_counter()
             mu, sg, cl, cu, info = hm.hotpix_fit(h, edges, sumMean, pstd, hotinfo)
+            self._host_time("hotpix_fit", t_fit)
             hotinfo.update(info)
             prm = HotpixParams()
             prm.mu, prm.sigma = float(mu), float(sg)
@@ -1045,9 +1058,11 @@ class Engine:
             ed = {"shiftsTriMat": shifts, "corrTriMat": corr, "originTriMat": orig, "peaksigTriMat": psig,
                   "translations": translations.copy()}
         else:
+            t_solve = time.perf_counter()
             ed = hm.solve_shifts(shifts, corr, psig, shapeImage=[P0, P1], maxShift=reg.maxShift,
                                  weightMode=reg.weightMode, peaksigThres=reg.peaksigThres, logisticK=reg.logisticK,
                                  logisticNu=reg.logisticNu)
+            self._host_time("drift_solve", t_solve)
             ed["originTriMat"] = orig
             if reg.weightMode == "autologistic":
                 out["peaksigThres"] = ed["peaksigThres"]
