@@ -37,8 +37,9 @@ int launched(const char* what) {
   return cuda_check(cudaGetLastError(), what);
 }
 
-// W_TWN^k = exp(-2 pi i k / TWN), one copy per device.
-static __device__ float2 d_twiddle[TWN];
+// W_TWN^k = exp(-2 pi i k / TWN), then its contiguous copies per
+// sub-transform length (tw_compact_off), one table per device.
+static __device__ float2 d_twiddle[TWN + TW_COMPACT];
 
 static std::mutex g_init_mu;
 static bool g_init_done[64];
@@ -51,10 +52,16 @@ static int init_device(int dev) {
   int prev = 0;
   ZR_TRY(cuda_check(cudaGetDevice(&prev), "cudaGetDevice"));
   if (prev != dev) ZR_TRY(cuda_check(cudaSetDevice(dev), "cudaSetDevice"));
-  static float2 host[TWN];
+  static float2 host[TWN + TW_COMPACT];
   for (int k = 0; k < TWN; k++) {
     const double a = -2.0 * M_PI * (double)k / (double)TWN;
     host[k] = make_float2((float)cos(a), (float)sin(a));
+  }
+  for (int k = 0; k < TW_COMPACT; k++) host[TWN + k] = make_float2(0.0f, 0.0f);
+  for (int M = 1; M <= 16384; M *= 2) {
+    for (int j = 0; j < M; j++) host[TWN + tw_compact_off(M) + j] = host[(size_t)j * (TWN / M)];
+    if (3 * M <= 12288)
+      for (int j = 0; j < 3 * M; j++) host[TWN + tw_compact_off(3 * M) + j] = host[(size_t)j * (TWN / (3 * M))];
   }
   int rc = cuda_check(cudaMemcpyToSymbol(d_twiddle, host, sizeof(host)), "twiddle upload");
   void* p = nullptr;

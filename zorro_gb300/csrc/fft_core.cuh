@@ -13,7 +13,8 @@
 //
 // Twiddles come from a table of W_TWN^k = exp(-2 pi i k / TWN), TWN = 2^14 x
 // 3^2 x 5, computed in double precision on the host and rounded to float
-// (``tw`` argument); a length-L transform reads every (TWN/L)-th entry.
+// (``tw`` argument); a length-L transform reads every (TWN/L)-th entry, or
+// the same values from a contiguous copy for its length (TW_COMPACT below).
 // DIR = -1 is the forward transform, +1 the inverse; neither is normalised.
 #pragma once
 #include <cuda_runtime.h>
@@ -22,6 +23,21 @@
 namespace zr {
 
 constexpr int TWN = 737280;  // twiddle table length: 2^14 * 3^2 * 5
+
+// After the TWN entries the table holds contiguous copies of it for the
+// sub-transform lengths M that the passes twiddle with: W_M^j (j < M) at
+// tw[TWN + tw_compact_off(M) + j], the same value as tw[j * (TWN / M)], for
+// M a power of two up to 16384 (offset M) and M = 3 * 2^a up to 12288
+// (offset 32768 + M).  A pass's twiddles W_M^(r k) for the consecutive k of
+// a warp's lanes then come from a few consecutive cache lines instead of one
+// line per lane of the strided table (a 4096-point pass would otherwise
+// touch about 1500 lines, more than the L1 left beside the shared memory).
+constexpr int TW_COMPACT = 32768 + 2 * 12288;
+__host__ __device__ constexpr bool tw_is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+__host__ __device__ constexpr int tw_compact_off(int M) {
+  return (tw_is_pow2(M) && M <= 16384) ? M
+                                       : ((M % 3 == 0 && tw_is_pow2(M / 3) && M <= 12288) ? 32768 + M : -1);
+}
 
 __host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 4); }
 // Row pitch of one sequence: the padded length rounded so that pitch = 4
@@ -181,27 +197,31 @@ constexpr int fft_radix(int rem) {
 // few powers from the table, the others as products of two table values (one
 // extra rounding), which keeps the load/store pipe for the data.
 template <int R, int DIR, int TWS>
-__device__ __forceinline__ void apply_twiddles(float2* v, int k, const float2* __restrict__ tw) {
+__device__ __forceinline__ void apply_twiddles(float2* v, int k, const float2* __restrict__ twtab) {
   auto twiddle = [&](int r, float2 ww) {
     if (DIR > 0) ww.y = -ww.y;
     v[r] = cmul(v[r], ww);
   };
-  const float2 w1 = __ldg(tw + k * TWS);
+  // W_M^(r k), M = TWN / TWS: from the contiguous copy when there is one
+  constexpr int OFF = tw_compact_off(TWN / TWS);
+  const float2* __restrict__ tw = OFF >= 0 ? twtab + TWN + OFF : twtab;
+  constexpr int ST = OFF >= 0 ? 1 : TWS;
+  const float2 w1 = __ldg(tw + k * ST);
   if constexpr (R == 2) {
     twiddle(1, w1);
   } else if constexpr (R == 3 || R == 5) {
     twiddle(1, w1);
 #pragma unroll
-    for (int r = 2; r < R; r++) twiddle(r, __ldg(tw + r * k * TWS));
+    for (int r = 2; r < R; r++) twiddle(r, __ldg(tw + r * k * ST));
   } else {
-    const float2 w2 = __ldg(tw + 2 * k * TWS);
-    const float2 w3 = (R == 16) ? __ldg(tw + 3 * k * TWS) : cmul(w1, w2);
+    const float2 w2 = __ldg(tw + 2 * k * ST);
+    const float2 w3 = (R == 16) ? __ldg(tw + 3 * k * ST) : cmul(w1, w2);
     twiddle(1, w1);
     twiddle(2, w2);
     twiddle(3, w3);
 #pragma unroll
     for (int a = 4; a < R; a += 4) {
-      const float2 wa = __ldg(tw + a * k * TWS);
+      const float2 wa = __ldg(tw + a * k * ST);
       twiddle(a, wa);
       twiddle(a + 1, cmul(R == 16 ? wa : w1, R == 16 ? w1 : wa));
       twiddle(a + 2, cmul(w2, wa));
