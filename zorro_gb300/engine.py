@@ -716,6 +716,7 @@ class Engine:
 
         # ---- hot pixels (zorro.py:2497-2672)
         ha = hb = None
+        hot_counts = None
         if "hot" in filt:
             bench["hot0"] = time.time()
             usum = self.tensor(pfx + "usum", (H, W), torch.float32)
@@ -748,10 +749,11 @@ class Engine:
             wb = self.lib.zr_hotpix_work_bytes(H, W)
             self.call("B_hot_maps", "zr_hotpix_maps", usum.data_ptr(), H, W, N, C.byref(prm), ha.data_ptr(), hb.data_ptr(),
                       cnt.data_ptr(), self.ptr(pfx + "hotwork", wb), wb, st)
-            c = cnt.cpu().numpy()
-            hotinfo["guessDeadpix"] = int(c[0])
-            hotinfo["guessHotpix"] = int(c[1])
-            hotinfo["neighborPix"] = int(c[2])
+            # the dead, hot and neighbour counts are only reported: they are
+            # read once the peaks are on the host, so no synchronisation holds
+            # back the spectra (the keys keep their place in hotpixInfo)
+            hot_counts = cnt
+            hotinfo["guessDeadpix"] = hotinfo["guessHotpix"] = hotinfo["neighborPix"] = None
             hotinfo["frameMean"] = float(mu / N)
             hotinfo["frameStd"] = float(sg / np.sqrt(N))
             frames = self._frames(raw, rtype, gain, ha, hb, gdiv)
@@ -804,7 +806,7 @@ class Engine:
         job = types.SimpleNamespace(
             reg=reg, pfx=pfx, bench=bench, raw=raw, gain=gain, rtype=rtype, gdiv=gdiv, N=N, H=H, W=W, frames=frames,
             pixelsize=pixelsize, hotinfo=hotinfo, filt=filt, ha=ha, hb=hb, P0=P0, P1=P1, C0=C0, C1=C1, mS=mS, w=w,
-            mask_dev=mask_dev, user_mask=user_mask, msub=msub,
+            mask_dev=mask_dev, user_mask=user_mask, msub=msub, hot_counts=hot_counts,
             half=str(getattr(reg, "spectraPrecision", "float32")).lower() in ("float16", "half", "f16"),
             refine=reg.triMode == "refine", preshift=bool(reg.preShift and mS))
         if job.half and job.refine:
@@ -1026,6 +1028,10 @@ class Engine:
         pairs, pr, keep = job.pairs, job.pr, job.keep
         filt, hotinfo, frames, pixelsize, user_mask = job.filt, job.hotinfo, job.frames, job.pixelsize, job.user_mask
         refine = job.refine
+        if job.hot_counts is not None:  # complete: the peaks came back after them on this stream
+            c = job.hot_counts.cpu().numpy()
+            hotinfo["guessDeadpix"], hotinfo["guessHotpix"], hotinfo["neighborPix"] = int(c[0]), int(c[1]), int(c[2])
+            job.hot_counts = None
         shifts = np.zeros([N, N, 2])
         corr = np.zeros([N, N])
         psig = np.zeros([N, N])
