@@ -134,6 +134,52 @@ def read_traffic():
     return out
 
 
+def movie_timeline(eng, torch, run):
+    """One more movie, outside the timed region, with every stage call
+    bracketed by CUDA events and the host steps stamped: the movie's time,
+    the union of the stage calls' device intervals (GPU busy), and the idle
+    gaps with the host steps that overlapped them.  Device and host times
+    share a base: an event recorded on an idle GPU at a known host time."""
+    import time as _t
+    eng.profile = {}
+    torch.cuda.synchronize()
+    base = torch.cuda.Event(enable_timing=True)
+    base.record()
+    torch.cuda.synchronize()
+    t0 = _t.perf_counter()
+    run()
+    end = torch.cuda.Event(enable_timing=True)
+    end.record()
+    torch.cuda.synchronize()
+    prof, hosts = eng.profile, eng.host_intervals()
+    eng.profile = None
+    ivs = sorted((base.elapsed_time(a), base.elapsed_time(b)) for k, v in prof.items()
+                 if not k.startswith("host:") for a, b in v)
+    busy = []
+    for a, b in ivs:
+        if busy and a <= busy[-1][1]:
+            busy[-1][1] = max(busy[-1][1], b)
+        else:
+            busy.append([a, b])
+    total = base.elapsed_time(end)
+    hs = [(k, (a - t0) * 1e3, (b - t0) * 1e3) for k, a, b in hosts]
+    gaps, prev = [], 0.0
+    for a, b in busy + [[total, total]]:
+        if a - prev > 0.1:
+            during = sorted({k for k, ha, hb in hs if ha < a and hb > prev})
+            gaps.append({"from_ms": round(prev, 2), "ms": round(a - prev, 2), "host": during})
+        prev = max(prev, b)
+    busy_ms = sum(b - a for a, b in busy)
+    idle_host = {}
+    for g in gaps:
+        key = "+".join(g["host"]) or "launch/sync"
+        idle_host[key] = round(idle_host.get(key, 0.0) + g["ms"], 2)
+    return {"movie_ms": round(total, 2), "gpu_busy_ms": round(busy_ms, 2), "gpu_idle_ms": round(total - busy_ms, 2),
+            "idle_ms_by_host_step": idle_host,
+            "host_steps": [{"step": k, "from_ms": round(a, 2), "ms": round(b - a, 2)} for k, a, b in hs],
+            "gaps_over_0.1ms": gaps}
+
+
 def slowest_rank(t_local, dist=None, device="cpu"):
     """Seconds per step of the job: the maximum over ranks of each rank's
     own time (each rank registers its own movies; no data-path collective)."""
@@ -873,6 +919,9 @@ def main():
             "fp32_peak_tflops": round(fp32_peak, 1),
             "host_ms_per_step": {k: round(v / args.steps, 3) for k, v in sorted(host_ms.items())}}
 
+    # ---- where one movie's time goes: device busy and idle, host steps
+    timeline = movie_timeline(eng, torch, lambda: make_reg(raw_dev, gain_dev, True).alignImageStack())
+
     # ---- accuracy of the last timed movie (outside the timed region): against
     # the known drift, and against the float64 oracle's outputs for this
     # seeded movie (tests/golden/oracle_<workload>.npz)
@@ -907,6 +956,7 @@ def main():
                 "wall_s_timed": round(wall, 3),
                 "clocks": clk.summary(),
                 "roofline": roof,
+                "timeline": timeline,
                 "accuracy": accuracy,
                 "cpu_baseline": cpu}
         if not args.profile_only:

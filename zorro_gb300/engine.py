@@ -118,12 +118,18 @@ class Engine:
     def host_ms(self):
         """Summed host time of the host steps (CDF fits, drift solves) while
         profiling was on."""
-        return {k[5:]: 1e3 * sum(v) for k, v in (self.profile or {}).items() if k.startswith("host:")}
+        return {k[5:]: 1e3 * sum(b - a for a, b in v) for k, v in (self.profile or {}).items()
+                if k.startswith("host:")}
+
+    def host_intervals(self):
+        """(step, start, end) of every host step while profiling was on, in
+        time.perf_counter seconds."""
+        return sorted((k[5:], a, b) for k, v in (self.profile or {}).items() if k.startswith("host:") for a, b in v)
 
     def _host_time(self, step, t0):
         if self.profile is not None:
             with self._profile_lock:
-                self.profile.setdefault("host:" + step, []).append(time.perf_counter() - t0)
+                self.profile.setdefault("host:" + step, []).append((t0, time.perf_counter()))
 
     # ------------------------------------------------------------------ planning
     def plan(self, P0, P1, C0, C1, mS, effort="FFTW_MEASURE", cache_dir=None):
