@@ -25,16 +25,25 @@
 
 namespace zr {
 
-constexpr int PK_T = 1024;
+// Threads of a peak-search CTA, and rows per thread of the vectorised filter
+// pass (register blocking of its vertical taps: the R rows of a thread share
+// each 16-byte row load).
+#ifndef ZR_PK_T
+#define ZR_PK_T 1024
+#endif
+#ifndef ZR_PK_VR
+#define ZR_PK_VR 2
+#endif
+constexpr int PK_T = ZR_PK_T;
 constexpr int PK_NW = PK_T / 32;  // warps
-constexpr int PK_RB = 16;      // rows per vertical-filter block
+constexpr int PK_RB = PK_T / 64;  // rows per block of the scalar filter pass
 constexpr int PK_MAXR = 64;    // largest filter radius
 constexpr int PK_SUBR = 8;     // +/- patch half-size (zorro.py:619)
 
 struct PkShared {
   double gw[2 * PK_MAXR + 1];
-  float wy[2 * PK_MAXR + 1];
-  float wx[2 * PK_MAXR + 1];
+  alignas(16) float wy[2 * PK_MAXR + 4];  // 16-byte aligned: read four taps at a time
+  alignas(16) float wx[2 * PK_MAXR + 4];
   double red[PK_NW][3];
   float redf[PK_NW];
   int redi[PK_NW];
@@ -258,34 +267,71 @@ __device__ void filter_pass(const float* C, float* V, const int* rtab, int w, in
 // filters 4 consecutive columns; the vertical taps are float4 loads, the
 // horizontal taps slide a 4-wide register window one column at a time.
 // Rows per thread of the vectorised filter pass (register blocking of the
-// vertical pass): 2, which keeps a thread within the 64 registers of a
-// 1024-thread CTA.
-__host__ __device__ constexpr int pk_vec_rows(int) { return 2; }
+// vertical pass): 2 by default, which keeps a thread within the 64
+// registers of a 1024-thread CTA.  The thread layout fixes the order in
+// which the filter statistics are summed, so it is part of the results.
+__host__ __device__ constexpr int pk_vec_rows(int) { return ZR_PK_VR; }
 __host__ __device__ constexpr int pk_vec_pitch(int w) { return w + 8; }
 
 // Horizontal pass of one row for 4 consecutive outputs x0..x0+3 away from
 // the borders: 16-byte loads of the row (p = row + x0 - rx - OFF is 16-byte
 // aligned), taps in order, the same fused multiply-adds as the scalar form.
+// Taps k0..k0+3 of the four outputs from the 12 values s = (A, B, Cn) that
+// start at tap k0's first input, weights W = wx[k0..k0+3].
+template <int OFF>
+__device__ __forceinline__ void taps4(const float4& A, const float4& B, const float4& Cn, const float4& W, float& f0,
+                                      float& f1, float& f2, float& f3) {
+  const float sv[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, Cn.x, Cn.y, Cn.z, Cn.w};
+  const float wv[4] = {W.x, W.y, W.z, W.w};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    f0 = fmaf(wv[q], sv[OFF + q], f0);
+    f1 = fmaf(wv[q], sv[OFF + q + 1], f1);
+    f2 = fmaf(wv[q], sv[OFF + q + 2], f2);
+    f3 = fmaf(wv[q], sv[OFF + q + 3], f3);
+  }
+}
+
 template <int OFF>
 __device__ __forceinline__ void hrow4(const float* __restrict__ p, const float* __restrict__ wx, int rx, float& f0,
                                       float& f1, float& f2, float& f3) {
+  const int K = 2 * rx;  // last tap
   float4 A = *reinterpret_cast<const float4*>(p), B = *reinterpret_cast<const float4*>(p + 4);
-  for (int k0 = 0; k0 <= 2 * rx; k0 += 4) {
+  int k0 = 0;
+  // eight taps a step while they are all there: no per-tap tests, the weights
+  // four at a time, the row chunks renamed rather than moved
+  for (; k0 + 7 <= K; k0 += 8) {
     const float4 Cn = *reinterpret_cast<const float4*>(p + k0 + 8);
-    const float s[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, Cn.x, Cn.y, Cn.z, Cn.w};
+    taps4<OFF>(A, B, Cn, *reinterpret_cast<const float4*>(wx + k0), f0, f1, f2, f3);
+    const float4 Dn = *reinterpret_cast<const float4*>(p + k0 + 12);
+    taps4<OFF>(B, Cn, Dn, *reinterpret_cast<const float4*>(wx + k0 + 4), f0, f1, f2, f3);
+    A = Cn;
+    B = Dn;
+  }
+  for (; k0 <= K; k0 += 4) {
+    const float4 Cn = *reinterpret_cast<const float4*>(p + k0 + 8);
+    const float sv[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, Cn.x, Cn.y, Cn.z, Cn.w};
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-      if (k0 + q <= 2 * rx) {
+      if (k0 + q <= K) {
         const float wk = wx[k0 + q];
-        f0 = fmaf(wk, s[OFF + q], f0);
-        f1 = fmaf(wk, s[OFF + q + 1], f1);
-        f2 = fmaf(wk, s[OFF + q + 2], f2);
-        f3 = fmaf(wk, s[OFF + q + 3], f3);
+        f0 = fmaf(wk, sv[OFF + q], f0);
+        f1 = fmaf(wk, sv[OFF + q + 1], f1);
+        f2 = fmaf(wk, sv[OFF + q + 2], f2);
+        f3 = fmaf(wk, sv[OFF + q + 3], f3);
       }
     }
     A = B;
     B = Cn;
   }
+}
+
+__device__ __forceinline__ float4 fma4(float w, const float4& v, float4 a) {
+  a.x = fmaf(w, v.x, a.x);
+  a.y = fmaf(w, v.y, a.y);
+  a.z = fmaf(w, v.z, a.z);
+  a.w = fmaf(w, v.w, a.w);
+  return a;
 }
 
 // Vectorised form for w % 4 == 0: w/4 column lanes of 4 columns, RB lanes of
@@ -320,6 +366,37 @@ __device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, i
       float wr[R];
 #pragma unroll
       for (int j = 0; j < R; j++) wr[j] = 0.0f;
+      if (R == 2 && yin) {
+        // rows y and y + 1 away from the borders: input row y - ry + t adds
+        // wy[t] to row y and wy[t - 1] to row y + 1, taps in order (as below),
+        // two input rows a step with no per-tap tests
+        const float* pr = C + (y - ry) * w + x0;
+        const int K = 2 * ry;
+        float4 a0 = acc[0], a1 = acc[R - 1];
+        float wp = wy[0];
+        a0 = fma4(wp, *reinterpret_cast<const float4*>(pr), a0);
+        int t = 1;
+        for (; t + 1 <= K; t += 2) {
+          const float4 va = *reinterpret_cast<const float4*>(pr + t * w);
+          const float4 vb = *reinterpret_cast<const float4*>(pr + (t + 1) * w);
+          const float wa = wy[t], wb = wy[t + 1];
+          a0 = fma4(wa, va, a0);
+          a1 = fma4(wp, va, a1);
+          a0 = fma4(wb, vb, a0);
+          a1 = fma4(wa, vb, a1);
+          wp = wb;
+        }
+        if (t <= K) {
+          const float4 va = *reinterpret_cast<const float4*>(pr + t * w);
+          const float wa = wy[t];
+          a0 = fma4(wa, va, a0);
+          a1 = fma4(wp, va, a1);
+          wp = wa;
+        }
+        a1 = fma4(wp, *reinterpret_cast<const float4*>(pr + (K + 1) * w), a1);
+        acc[0] = a0;
+        acc[R - 1] = a1;
+      } else
       for (int t = 0; t <= 2 * ry + R - 1; t++) {
         // wr[j] = wy[t - j]
 #pragma unroll
