@@ -788,14 +788,20 @@ def main():
         h0 = torch.cuda.Event(enable_timing=True)
         h1 = torch.cuda.Event(enable_timing=True)
         h0.record()
+        last16 = None
         for _ in range(args.steps):
-            make_reg16().alignImageStack()
+            last16 = make_reg16()
+            last16.alignImageStack()
         h1.record()
         barrier()
         t16 = slowest_rank(h0.elapsed_time(h1) / 1000.0 / args.steps, dist, dev)
         fp16 = {"value": round(world / t16, 3), "unit": UNIT, "ms_per_step": round(t16 * 1e3, 3),
                 "spectra_bytes_half": int(2 * N * (Cc // 2 + 1) * Cc * 4),
                 "spectra_bytes_float": int(2 * N * (Cc // 2 + 1) * Cc * 8)}
+        if rank == 0:
+            # the half-precision movie against the float64 oracle's outputs
+            fp16["accuracy"] = {k: v for k, v in oracle_accuracy(args.workload, mv, last16).items()
+                                if k != "vs_fp64_oracle"}
 
     # ---- served path: movies in flight in parallel slots (continuous batching)
     from zorro_gb300.serve import MovieServer
