@@ -1058,6 +1058,7 @@ class Engine:
         # ---- drift solve (shiftsSolver zorro.py:1260-1567)
         out = {}
         edl = list(reg.errorDictList)
+        finish_errors = None
         if reg.triMode == "first":
             translations = -shifts[0, :]
             ed = {"shiftsTriMat": shifts, "corrTriMat": corr, "originTriMat": orig, "peaksigTriMat": psig,
@@ -1071,16 +1072,17 @@ class Engine:
                   "translations": translations.copy()}
         else:
             t_solve = time.perf_counter()
-            ed = hm.solve_shifts(shifts, corr, psig, shapeImage=[P0, P1], maxShift=reg.maxShift,
-                                 weightMode=reg.weightMode, peaksigThres=reg.peaksigThres, logisticK=reg.logisticK,
-                                 logisticNu=reg.logisticNu)
+            # the error analysis of the solve waits until the shifted sums are
+            # queued (finish_errors below): only the translations gate them
+            ed, trans, finish_errors = hm.solve_shifts(
+                shifts, corr, psig, shapeImage=[P0, P1], maxShift=reg.maxShift, weightMode=reg.weightMode,
+                peaksigThres=reg.peaksigThres, logisticK=reg.logisticK, logisticNu=reg.logisticNu, defer_errors=True)
             self._host_time("drift_solve", t_solve)
-            ed["originTriMat"] = orig
             if reg.weightMode == "autologistic":
                 out["peaksigThres"] = ed["peaksigThres"]
                 out["logisticK"] = ed["logisticK"]
                 out["logisticNu"] = ed["logisticNu"]
-            translations = ed["translations"].copy()
+            translations = trans.copy()
         edl.append(ed)
         out["errorDictList"] = edl
         bench["solve1"] = time.time()
@@ -1129,6 +1131,9 @@ class Engine:
                 self.call("I_dose", "zr_dose_filter", aligned.data_ptr(), N, H, W, C.byref(dp), tq.data_ptr(), de.data_ptr(),
                           P0, P1, filt_sum.data_ptr(), self.ptr(pfx + "dosework", dwb), dwb, st)
         bench["dose1"] = time.time()
+        if finish_errors is not None:  # while the GPU shifts, sums and filters
+            finish_errors()
+            ed["originTriMat"] = orig
 
         job.translations, job.isum, job.esum, job.osum = translations, isum, esum, osum
         job.aligned, job.aligned_ready, job.filt_sum = aligned, aligned_ready, filt_sum

@@ -10,7 +10,9 @@ follows.  The GPU does every pass over pixels.
 from __future__ import annotations
 
 import concurrent.futures
+import functools
 import math
+import threading
 
 import numpy as np
 import scipy.optimize
@@ -133,10 +135,27 @@ def logistic_fit(peaksigTriMat):
             "hSigma": hSigma}
 
 
+_L1_POOL = None
+_L1_LOCK = threading.Lock()
+
+
+def _l1_pool():
+    """Threads for the y-axis solves (the native solver releases the GIL),
+    kept for the process."""
+    global _L1_POOL
+    with _L1_LOCK:
+        if _L1_POOL is None:
+            _L1_POOL = concurrent.futures.ThreadPoolExecutor(4, thread_name_prefix="zorro-l1")
+        return _L1_POOL
+
+
 def solve_shifts(shiftsTriMat_in, corrTriMat_in, peaksigTriMat_in, *, shapeImage, maxShift, weightMode,
-                 peaksigThres, logisticK, logisticNu):
+                 peaksigThres, logisticK, logisticNu, defer_errors=False):
     """The drift solve and its error analysis.  zorro.py:1260-1567.
-    Returns the errorDict (its 'translations' are the frame shifts to apply)."""
+    Returns the errorDict (its 'translations' are the frame shifts to apply).
+    With ``defer_errors`` it returns (errorDict so far, translations,
+    finish): the caller can use the translations at once and call finish()
+    later to add the error analysis (the same values, in the same order)."""
     sh = shiftsTriMat_in[:-1, 1:, :]
     co = corrTriMat_in[:-1, 1:]
     ps = peaksigTriMat_in[:-1, 1:]
@@ -171,11 +190,20 @@ def solve_shifts(shiftsTriMat_in, corrTriMat_in, peaksigTriMat_in, *, shapeImage
     weff = weights * accepted
     # the x and y solves are independent: y on a helper thread (the native
     # solver releases the GIL) while x runs here
-    with concurrent.futures.ThreadPoolExecutor(1) as ex:
-        fy = ex.submit(l1_solve, A, b_y, weff, -lim, lim)
-        rel[:, 1] = l1_solve(A, b_x, weff, -lim, lim)
-        rel[:, 0] = fy.result()
-    # weighted error analysis, zorro.py:1484-1547
+    fy = _l1_pool().submit(l1_solve, A, b_y, weff, -lim, lim)
+    rel[:, 1] = l1_solve(A, b_x, weff, -lim, lim)
+    rel[:, 0] = fy.result()
+    translations = -np.vstack((np.zeros([1, 2]), np.cumsum(rel, axis=0)))
+    finish = functools.partial(_error_analysis, ed, A, rel, b_x, b_y, weights, accepted, N, unrav, M, translations,
+                               shiftsTriMat_in)
+    if defer_errors:
+        return ed, translations, finish
+    return finish()
+
+
+def _error_analysis(ed, A, rel, b_x, b_y, weights, accepted, N, unrav, M, translations, shiftsTriMat_in):
+    """The weighted error analysis of the drift solve (zorro.py:1484-1547),
+    completing its errorDict."""
     weights = np.clip(weights, 1e-6, np.inf)
     errorXY = np.stack([A @ rel[:, 0] - b_y, A @ rel[:, 1] - b_x], axis=1)
     errorNorm = np.sqrt(errorXY[:, 0] ** 2 + errorXY[:, 1] ** 2)
@@ -206,7 +234,7 @@ def solve_shifts(shiftsTriMat_in, corrTriMat_in, peaksigTriMat_in, *, shapeImage
         den = row_col(wu)
         errorX = row_col(ex * wu) / den
         errorY = row_col(ey * wu) / den
-    ed.update({"translations": -np.vstack((np.zeros([1, 2]), np.cumsum(rel, axis=0))), "relativeEst": rel,
+    ed.update({"translations": translations, "relativeEst": rel,
                "acceptedEqns": accepted, "weights": weights, "errorXY": errorXY, "shiftsTriMat": shiftsTriMat_in,
                "errorX": errorX, "errorY": errorY, "errorUnraveled": errorUnraveled, "mean_errorNorm": mean_e,
                "std_errorNorm": std_e, "M": M, "Maccepted": M})
