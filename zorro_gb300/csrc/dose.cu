@@ -48,9 +48,12 @@ __global__ void __launch_bounds__(fft_threads(P1, ds_nbr(P1)), ds_minb(fft_threa
   const int na = f0 + 2 * pl, nb = na + 1;
   const float* ia = img + (size_t)na * H * W;
   const float* ib = img + (size_t)(nb < N ? nb : na) * H * W;
-  // element x of row r: the symmetric padding of the two frames' row
-  block_fft_from<P1, ds_nbr(P1), T, -1>(sm, tw, [&](int r, int x) {
-    const int yy = g * ds_nbr(P1) + r;
+  // element x of row r: the symmetric padding of the two frames' row; every
+  // pass but the last, which pairs X[k] with X[P1 - k] in registers
+  constexpr int NB = ds_nbr(P1);
+  constexpr int RL = last_radix(P1), NSL = P1 / RL;
+  block_fft_from<P1, NB, T, -1, NSL>(sm, tw, [&](int r, int x) {
+    const int yy = g * NB + r;
     const int ys = yy < H ? yy : (yy < 2 * H ? 2 * H - 1 - yy : sym_idx(yy, H));
     const int xs = x < W ? x : (x < 2 * W ? 2 * W - 1 - x : sym_idx(x, W));
     const size_t p = (size_t)ys * W + xs;
@@ -59,18 +62,26 @@ __global__ void __launch_bounds__(fft_threads(P1, ds_nbr(P1)), ds_minb(fft_threa
   // output: column-major per frame, [frame][kx][ky]
   const size_t fa = (size_t)(2 * pl) * K4 * P0;
   const size_t fb = fa + (size_t)K4 * P0;
-  for (int e = threadIdx.x; e < K4 * ds_nbr(P1); e += T) {
-    const int k = e / ds_nbr(P1), r = e - k * ds_nbr(P1);
-    const size_t o = (size_t)k * P0 + g * ds_nbr(P1) + r;
-    float2 U = make_float2(0.0f, 0.0f), V = U;
-    if (k <= P1 / 2) {
-      const float2 zk = sm[r * LD + pidx(k)];
-      const float2 zm = sm[r * LD + pidx(k == 0 ? 0 : P1 - k)];
-      U = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-      V = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+  const int y0 = g * NB;
+  fft_last_paired<P1, NB, T, -1>(sm, tw, [&](int r, int k0, const float2* x0, int k1, const float2* x1) {
+    auto put = [&](int k, float2 zk, float2 zm) {
+      const size_t o = (size_t)k * P0 + y0 + r;
+      RW[fa + o] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      if (nb < N) RW[fb + o] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    };
+#pragma unroll
+    for (int q = 0; q < RL; q++) {
+      const int m0 = k0 + q * NSL, m1 = k1 + q * NSL;
+      if (m0 <= P1 / 2) put(m0, x0[q], k0 > 0 ? x1[RL - 1 - q] : x0[(RL - q) % RL]);
+      if (m1 <= P1 / 2) put(m1, x1[q], k0 > 0 ? x0[RL - 1 - q] : x1[RL - 1 - q]);
     }
-    RW[fa + o] = U;
-    if (nb < N) RW[fb + o] = V;
+  });
+  // the pitch's columns past P1/2 are zero
+  for (int e = threadIdx.x; e < NB * (K4 - P1 / 2 - 1); e += T) {
+    const int r = e % NB, k = P1 / 2 + 1 + e / NB;
+    const size_t o = (size_t)k * P0 + y0 + r;
+    RW[fa + o] = make_float2(0.0f, 0.0f);
+    if (nb < N) RW[fb + o] = make_float2(0.0f, 0.0f);
   }
 }
 
@@ -136,23 +147,37 @@ __global__ void __launch_bounds__(DS_CT, 2)
     fm[j] = (first || !prm.normalize) ? 0.0f : FM[(size_t)kx * P0 + y];
   }
   const float LOG2E = 1.4426950408889634f;
+  // the last pass's butterfly j = thread holds elements j + r P0/R: with
+  // P0/R = DS_CT those are exactly the thread's accumulator rows, so the
+  // spectrum is weighted and summed straight from its registers
+  constexpr bool ACC_DIRECT = P0 / last_radix(P0) == DS_CT && last_radix(P0) == PER;
   for (int nl = 0; nl < nfr; nl++) {
     const float2* col = RW + ((size_t)nl * K4 + kx) * P0;
-    __syncthreads();  // the previous frame's spectrum has been read
-    block_fft_from<P0, 1, DS_CT, -1>(sm, tw, [&](int, int y) { return __ldg(col + y); });
-    if (!live) continue;
     // filt = exp(-0.5 D / crit), thres = exp(-(q / thresQ)^order)
     const float cd = (-0.5f * dose_end[f0 + nl]) * LOG2E;
     const float ltq = log2f(thres_q[f0 + nl]);
-#pragma unroll
-    for (int j = 0; j < PER; j++) {
-      const int y = threadIdx.x + j * DS_CT;
+    auto accumulate = [&](int j, int y, float2 F) {
       const float filt = exp2f(cd * inv_crit[y]);
       const float thres = exp2f(-LOG2E * exp2f(prm.cutoff_order * (lq[y] - ltq)));
       const float w = thres * filt;
-      const float2 F = sm[pidx(y)];
       acc[j] = make_float2(acc[j].x + F.x * w, acc[j].y + F.y * w);
       if (prm.normalize) fm[j] += w;
+    };
+    __syncthreads();  // the previous frame's spectrum has been read
+    if constexpr (ACC_DIRECT) {
+      block_fft_from<P0, 1, DS_CT, -1>(
+          sm, tw, [&](int, int y) { return __ldg(col + y); },
+          all_out([&](int, int y, int r, float2 F) {
+            if (live) accumulate(r, y, F);
+          }));
+    } else {
+      block_fft_from<P0, 1, DS_CT, -1>(sm, tw, [&](int, int y) { return __ldg(col + y); });
+      if (!live) continue;
+#pragma unroll
+      for (int j = 0; j < PER; j++) {
+        const int y = threadIdx.x + j * DS_CT;
+        accumulate(j, y, sm[pidx(y)]);
+      }
     }
   }
 #pragma unroll

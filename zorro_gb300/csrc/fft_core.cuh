@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace zr {
 
 constexpr int TWN = 737280;  // twiddle table length: 2^14 * 3^2 * 5
@@ -230,22 +232,58 @@ __device__ __forceinline__ void apply_twiddles(float2* v, int k, const float2* _
   }
 }
 
+// Where the last pass puts its outputs: by default back in shared memory
+// (natural order).  An output functor ``out`` instead receives them in
+// registers: ``out.need(b, k)`` says whether any output k + r L/R (r < R) of
+// sequence b is kept (the butterflies of the others are skipped) and
+// ``out(b, i, r, v)`` is called for every output i = k + r L/R of a needed
+// butterfly, so the kept elements go straight to global memory (or into the
+// caller's registers) without another store, barrier and load in shared
+// memory.
+struct SmemOut {};
+
+// An output functor that keeps every butterfly, around a callable f(b, i, r, v).
+template <typename F>
+struct AllOut {
+  F f;
+  __device__ __forceinline__ bool need(int, int) const { return true; }
+  __device__ __forceinline__ void operator()(int b, int i, int r, float2 v) const { f(b, i, r, v); }
+};
+template <typename F>
+__device__ __forceinline__ AllOut<F> all_out(F f) { return AllOut<F>{f}; }
+
+// Radix of the last pass of a length-L transform.
+constexpr int last_radix(int L) {
+  int rem = L;
+  int r = fft_radix(rem);
+  while (rem > r) {
+    rem /= r;
+    r = fft_radix(rem);
+  }
+  return r;
+}
+
 // One Stockham pass (radix R, NS = product of the radices already applied),
-// then the remaining passes.
-template <int L, int NB, int T, int DIR, int NS>
-__device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ tw) {
+// then the remaining passes up to the one that would start at NS = STOP
+// (STOP = L: all of them).
+template <int L, int NB, int T, int DIR, int NS, typename Out = SmemOut, int STOP = L>
+__device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ tw, const Out& out = Out()) {
   constexpr int R = fft_radix(L / NS);
   constexpr int LR = L / R;
   constexpr int NBF = NB * LR;
   constexpr int K = (NBF + T - 1) / T;
   constexpr int LD = ld_of(L);
   constexpr int TWS = TWN / (NS * R);
+  constexpr bool DIRECT = NS * R == L && !std::is_same<Out, SmemOut>::value;
   float2 v[K][R];
 #pragma unroll
   for (int i = 0; i < K; i++) {
     const int bf = threadIdx.x + i * T;
     if ((NBF % T) == 0 || bf < NBF) {
       const int b = bf / LR, j = bf - (bf / LR) * LR;
+      if constexpr (DIRECT) {
+        if (!out.need(b, j)) continue;
+      }
       const float2* src = s + b * LD;
       const int k = j % NS;
 #pragma unroll
@@ -254,21 +292,35 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
       dft<R, DIR>(v[i]);
     }
   }
-  __syncthreads();
+  if constexpr (DIRECT) {
+    // last pass: j < NS, so output r of butterfly j is element j + r NS
 #pragma unroll
-  for (int i = 0; i < K; i++) {
-    const int bf = threadIdx.x + i * T;
-    if ((NBF % T) == 0 || bf < NBF) {
-      const int b = bf / LR, j = bf - (bf / LR) * LR;
-      float2* dst = s + b * LD;
-      const int k = j % NS;
-      const int base = (j / NS) * NS * R + k;
+    for (int i = 0; i < K; i++) {
+      const int bf = threadIdx.x + i * T;
+      if ((NBF % T) == 0 || bf < NBF) {
+        const int b = bf / LR, j = bf - (bf / LR) * LR;
+        if (!out.need(b, j)) continue;
 #pragma unroll
-      for (int r = 0; r < R; r++) dst[pidx(base + r * NS)] = v[i][r];
+        for (int r = 0; r < R; r++) out(b, j + r * NS, r, v[i][r]);
+      }
     }
+  } else {
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+      const int bf = threadIdx.x + i * T;
+      if ((NBF % T) == 0 || bf < NBF) {
+        const int b = bf / LR, j = bf - (bf / LR) * LR;
+        float2* dst = s + b * LD;
+        const int k = j % NS;
+        const int base = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) dst[pidx(base + r * NS)] = v[i][r];
+      }
+    }
+    __syncthreads();
+    if constexpr (NS * R < L && NS * R < STOP) fft_pass<L, NB, T, DIR, NS * R, Out, STOP>(s, tw, out);
   }
-  __syncthreads();
-  if constexpr (NS * R < L) fft_pass<L, NB, T, DIR, NS * R>(s, tw);
 }
 
 // block_fft of NB sequences whose elements come from ``load(b, i)`` (element
@@ -276,8 +328,9 @@ __device__ __forceinline__ void fft_pass(float2* s, const float2* __restrict__ t
 // butterflies straight from the loader, all of a thread's loads before any
 // arithmetic, and writes its outputs to ``s``; the other passes run in shared
 // memory.  Saves one store and one load of every element in shared memory.
-template <int L, int NB, int T, int DIR, typename Load>
-__device__ __forceinline__ void block_fft_from(float2* s, const float2* __restrict__ tw, Load load) {
+template <int L, int NB, int T, int DIR, int STOP = L, typename Load, typename Out = SmemOut>
+__device__ __forceinline__ void block_fft_from(float2* s, const float2* __restrict__ tw, Load load,
+                                               const Out& out = Out()) {
   static_assert(L >= 2 && TWN % L == 0, "L must divide the twiddle table length 2^14 * 3^2 * 5");
   constexpr int R = fft_radix(L);
   constexpr int LR = L / R;
@@ -305,7 +358,42 @@ __device__ __forceinline__ void block_fft_from(float2* s, const float2* __restri
     }
   }
   __syncthreads();
-  if constexpr (R < L) fft_pass<L, NB, T, DIR, R>(s, tw);
+  if constexpr (R < L && R < STOP) fft_pass<L, NB, T, DIR, R, Out, STOP>(s, tw, out);
+}
+
+// The last pass of a length-L transform (radix R = last_radix(L), NS = L/R,
+// after every other pass has run in shared memory) with the butterflies k
+// and NS - k of one sequence in the same thread (k = 0 with NS/2), so that
+// each output X[m] meets X[L - m] in registers: output r of butterfly k is
+// X[k + r NS], and X[L - k - r NS] is output R-1-r of butterfly NS - k (for
+// k = 0: output (R - r) mod R of butterfly 0).  For every unit (sequence b,
+// k) ``pair(b, k0, X0, k1, X1)`` receives the two butterflies' outputs.
+template <int L, int NB, int T, int DIR, typename Pair>
+__device__ __forceinline__ void fft_last_paired(const float2* s, const float2* __restrict__ tw, Pair pair) {
+  constexpr int R = last_radix(L);
+  constexpr int NS = L / R;
+  constexpr int LD = ld_of(L);
+  constexpr int TWS = TWN / L;
+  constexpr int NU = NB * (NS / 2);
+  static_assert(NS % 2 == 0, "paired last pass needs an even number of butterflies");
+  for (int t = threadIdx.x; t < NU; t += T) {
+    const int u = t / NB, b = t - (t / NB) * NB;  // neighbouring threads: the same k of the next sequence
+    const int k0 = u, k1 = u == 0 ? NS / 2 : NS - u;
+    const float2* src = s + b * LD;
+    float2 x0[R], x1[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      x0[r] = src[pidx(k0 + r * NS)];
+      x1[r] = src[pidx(k1 + r * NS)];
+    }
+    if (NS > 1) {
+      apply_twiddles<R, DIR, TWS>(x0, k0, tw);
+      apply_twiddles<R, DIR, TWS>(x1, k1, tw);
+    }
+    dft<R, DIR>(x0);
+    dft<R, DIR>(x1);
+    pair(b, k0, x0, k1, x1);
+  }
 }
 
 // Transform NB sequences of length L in shared memory (natural order in and

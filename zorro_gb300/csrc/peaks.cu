@@ -34,11 +34,20 @@ namespace zr {
 #ifndef ZR_PK_VR
 #define ZR_PK_VR 2
 #endif
+
 constexpr int PK_T = ZR_PK_T;
 constexpr int PK_NW = PK_T / 32;  // warps
 constexpr int PK_RB = PK_T / 64;  // rows per block of the scalar filter pass
 constexpr int PK_MAXR = 64;    // largest filter radius
 constexpr int PK_SUBR = 8;     // +/- patch half-size (zorro.py:619)
+
+// The bounded Brent search's state.  It lives in shared memory and only
+// thread 0 touches it, so none of it stays in registers across the filter
+// passes of the other threads.
+struct BrentState {
+  double a, b, fulc, nfc, xf, rat, e, x, fx, ffulc, fnfc, xm, tol1, tol2;
+  int num;
+};
 
 struct PkShared {
   double gw[2 * PK_MAXR + 1];
@@ -56,6 +65,7 @@ struct PkShared {
   int st_n;
   double x;             // the Brent search's next abscissa (thread 0 -> all)
   int go;               // 1 while the search continues
+  BrentState bs;        // the search's state (thread 0 only)
 };
 
 __device__ __forceinline__ int reflect_idx(int i, int n) {
@@ -419,12 +429,17 @@ __device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, i
     }
     __syncthreads();
     if (act) {
+      // the horizontal taps of the thread's R rows, then their statistics
+      float fr[R][4];
 #pragma unroll
       for (int j = 0; j < R; j++) {
-        const int yy = y + j;
-        if (yy >= w) break;
+        fr[j][0] = fr[j][1] = fr[j][2] = fr[j][3] = 0.f;
+        if (y + j >= w) break;
         const float* vr = V + (ty * R + j) * VP;
-        float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+        float& f0 = fr[j][0];
+        float& f1 = fr[j][1];
+        float& f2 = fr[j][2];
+        float& f3 = fr[j][3];
         if (xin) {
           const float* pp = vr + x0 - rx - OFF;
           switch (OFF) {
@@ -443,10 +458,14 @@ __device__ void filter_pass4(const float* C, float* V, const int* rtab, int w, i
             a0 = a1; a1 = a2; a2 = a3;
           }
         }
-        const float fv[4] = {f0, f1, f2, f3};
+      }
+#pragma unroll
+      for (int j = 0; j < R; j++) {
+        const int yy = y + j;
+        if (yy >= w) break;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-          const float f = fv[q];
+          const float f = fr[j][q];
           const int x = x0 + q;
           bool in = true;
           if (MODE == 1) {
@@ -512,93 +531,112 @@ __device__ __forceinline__ double sgn1(double v) { return v > 0.0 ? 1.0 : (v < 0
 // The search's scalar state lives in thread 0, which decides each next
 // abscissa and whether to go on and hands them to the CTA through shared
 // memory; all threads evaluate the objective.
+// Thread 0: the next abscissa of the search (sh.x, sh.go = 1), or its end
+// (sh.go = 0).
+__device__ void brent_next(BrentState& S, PkShared& sh) {
+  const double golden = 0.5 * (3.0 - sqrt(5.0));
+  if (!(fabs(S.xf - S.xm) > (S.tol2 - 0.5 * (S.b - S.a)))) {
+    sh.go = 0;
+    return;
+  }
+  bool gstep = true;
+  if (fabs(S.e) > S.tol1) {
+    gstep = false;
+    double r = (S.xf - S.nfc) * (S.fx - S.ffulc);
+    double q = (S.xf - S.fulc) * (S.fx - S.fnfc);
+    double p = (S.xf - S.fulc) * q - (S.xf - S.nfc) * r;
+    q = 2.0 * (q - r);
+    if (q > 0.0) p = -p;
+    q = fabs(q);
+    r = S.e;
+    S.e = S.rat;
+    if ((fabs(p) < fabs(0.5 * q * r)) && (p > q * (S.a - S.xf)) && (p < q * (S.b - S.xf))) {
+      S.rat = (p + 0.0) / q;
+      S.x = S.xf + S.rat;
+      if (((S.x - S.a) < S.tol2) || ((S.b - S.x) < S.tol2)) S.rat = S.tol1 * sgn1(S.xm - S.xf);
+    } else {
+      gstep = true;
+    }
+  }
+  if (gstep) {
+    S.e = (S.xf >= S.xm) ? (S.a - S.xf) : (S.b - S.xf);
+    S.rat = golden * S.e;
+  }
+  S.x = S.xf + sgn1(S.rat) * fmax(fabs(S.rat), S.tol1);
+  sh.x = S.x;
+  sh.go = 1;
+}
+
+// Bounded Brent minimisation (FMM FMIN).  Returns the abscissa of the best
+// value (to every thread); *nfev receives the number of function values.
+// Thread 0 runs the search (its state in shared memory), decides each next
+// abscissa and whether to go on and hands them to the CTA through shared
+// memory; all threads evaluate the objective.
 __device__ double fmin_bounded(const float* C, float* V, const int* rtab, int w, int mS, float c, PkShared& sh,
                                double lo, double hi, double xatol, int maxfun, int* nfev) {
   const bool lead = threadIdx.x == 0;
   const double sqrt_eps = sqrt(2.2e-16);
   const double golden = 0.5 * (3.0 - sqrt(5.0));
-  double a = lo, b = hi;
-  double fulc = a + golden * (b - a);
-  double nfc = fulc, xf = fulc;
-  double rat = 0.0, e = 0.0;
-  double x = xf;
-  double fx = objective(C, V, rtab, w, mS, x, c, sh);
-  int num = 1;
-  double ffulc = fx, fnfc = fx;
-  double xm = 0.5 * (a + b);
-  double tol1 = sqrt_eps * fabs(xf) + xatol / 3.0;
-  double tol2 = 2.0 * tol1;
-  // thread 0: the next abscissa of the loop below, or the end of the search
-  auto next_point = [&]() {
-    if (!(fabs(xf - xm) > (tol2 - 0.5 * (b - a)))) {
-      sh.go = 0;
-      return;
+  const double x0 = lo + golden * (hi - lo);
+  const double f0 = objective(C, V, rtab, w, mS, x0, c, sh);
+  if (lead) {
+    BrentState S;
+    S.a = lo;
+    S.b = hi;
+    S.fulc = x0;
+    S.nfc = x0;
+    S.xf = x0;
+    S.rat = 0.0;
+    S.e = 0.0;
+    S.x = x0;
+    S.fx = f0;
+    S.num = 1;
+    S.ffulc = f0;
+    S.fnfc = f0;
+    S.xm = 0.5 * (lo + hi);
+    S.tol1 = sqrt_eps * fabs(x0) + xatol / 3.0;
+    S.tol2 = 2.0 * S.tol1;
+    brent_next(S, sh);
+    if (!sh.go) {  // the search ended before its first step
+      sh.x = S.xf;
+      sh.bi[1] = S.num;
     }
-    bool gstep = true;
-    if (fabs(e) > tol1) {
-      gstep = false;
-      double r = (xf - nfc) * (fx - ffulc);
-      double q = (xf - fulc) * (fx - fnfc);
-      double p = (xf - fulc) * q - (xf - nfc) * r;
-      q = 2.0 * (q - r);
-      if (q > 0.0) p = -p;
-      q = fabs(q);
-      r = e;
-      e = rat;
-      if ((fabs(p) < fabs(0.5 * q * r)) && (p > q * (a - xf)) && (p < q * (b - xf))) {
-        rat = (p + 0.0) / q;
-        x = xf + rat;
-        if (((x - a) < tol2) || ((b - x) < tol2)) rat = tol1 * sgn1(xm - xf);
-      } else {
-        gstep = true;
-      }
-    }
-    if (gstep) {
-      e = (xf >= xm) ? (a - xf) : (b - xf);
-      rat = golden * e;
-    }
-    x = xf + sgn1(rat) * fmax(fabs(rat), tol1);
-    sh.x = x;
-    sh.go = 1;
-  };
-  if (lead) next_point();
+    sh.bs = S;
+  }
   __syncthreads();
   while (sh.go) {
     const double xe = sh.x;
     const double fu = objective(C, V, rtab, w, mS, xe, c, sh);  // barriers: every thread has read sh.x, sh.go
     if (lead) {
-      num += 1;
-      if (fu <= fx) {
-        if (x >= xf) a = xf; else b = xf;
-        fulc = nfc; ffulc = fnfc;
-        nfc = xf; fnfc = fx;
-        xf = x; fx = fu;
+      BrentState S = sh.bs;
+      S.num += 1;
+      if (fu <= S.fx) {
+        if (S.x >= S.xf) S.a = S.xf; else S.b = S.xf;
+        S.fulc = S.nfc; S.ffulc = S.fnfc;
+        S.nfc = S.xf; S.fnfc = S.fx;
+        S.xf = S.x; S.fx = fu;
       } else {
-        if (x < xf) a = x; else b = x;
-        if ((fu <= fnfc) || (nfc == xf)) {
-          fulc = nfc; ffulc = fnfc;
-          nfc = x; fnfc = fu;
-        } else if ((fu <= ffulc) || (fulc == xf) || (fulc == nfc)) {
-          fulc = x; ffulc = fu;
+        if (S.x < S.xf) S.a = S.x; else S.b = S.x;
+        if ((fu <= S.fnfc) || (S.nfc == S.xf)) {
+          S.fulc = S.nfc; S.ffulc = S.fnfc;
+          S.nfc = S.x; S.fnfc = fu;
+        } else if ((fu <= S.ffulc) || (S.fulc == S.xf) || (S.fulc == S.nfc)) {
+          S.fulc = S.x; S.ffulc = fu;
         }
       }
-      xm = 0.5 * (a + b);
-      tol1 = sqrt_eps * fabs(xf) + xatol / 3.0;
-      tol2 = 2.0 * tol1;
-      if (num >= maxfun) sh.go = 0;
-      else next_point();
+      S.xm = 0.5 * (S.a + S.b);
+      S.tol1 = sqrt_eps * fabs(S.xf) + xatol / 3.0;
+      S.tol2 = 2.0 * S.tol1;
+      if (S.num >= maxfun) sh.go = 0;
+      else brent_next(S, sh);
       if (!sh.go) {
-        sh.x = xf;
-        sh.bi[1] = num;
+        sh.x = S.xf;
+        sh.bi[1] = S.num;
       }
+      sh.bs = S;
     }
     __syncthreads();
   }
-  if (lead && num == 1) {  // the search ended before its first step
-    sh.x = xf;
-    sh.bi[1] = num;
-  }
-  __syncthreads();
   const double best = sh.x;
   *nfev = sh.bi[1];
   __syncthreads();
