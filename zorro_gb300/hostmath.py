@@ -494,6 +494,98 @@ def _value_and_gradient(f_rows, bounds, step=1e-8):
     return fg
 
 
+def _setulb_loop(fg, x0, bounds, m=10, ftol=2.2204460492503131e-09, gtol=1e-5, maxfun=15000, maxiter=15000,
+                 maxls=20):
+    """The iterates of scipy.optimize.minimize(fg, x0, method='L-BFGS-B',
+    jac=True, bounds=bounds) with its defaults: the same compiled step
+    routine (scipy.optimize._lbfgsb.setulb) driven by the same loop as
+    scipy's own driver, with f and g taken straight from ``fg`` (evaluated
+    once per new x, as scipy's ScalarFunction does) instead of through its
+    wrapper objects, whose Python overhead is most of the time of a small
+    fit.  Returns x.  The call signature is that of scipy's C port of
+    L-BFGS-B (scipy 1.15 and later); ``lbfgsb_minimize`` checks the result
+    against scipy.optimize.minimize before using it."""
+    from scipy.linalg.lapack import HAS_ILP64
+    from scipy.optimize import _lbfgsb
+    lb = np.array([float(b[0]) for b in bounds], dtype=np.float64)
+    ub = np.array([float(b[1]) for b in bounds], dtype=np.float64)
+    x = np.array(np.clip(np.asarray(x0).ravel(), lb, ub), dtype=np.float64)
+    n = x.size
+    it = np.int64 if HAS_ILP64 else np.int32
+    nbd = np.full(n, 2, dtype=it)  # both bounds finite
+    f = np.array(0.0, dtype=np.float64)
+    g = np.zeros(n, dtype=np.float64)
+    wa = np.zeros(2 * m * n + 5 * n + 11 * m * m + 8 * m, np.float64)
+    iwa = np.zeros(3 * n, dtype=it)
+    task = np.zeros(2, dtype=it)
+    ln_task = np.zeros(2, dtype=it)
+    lsave = np.zeros(4, dtype=it)
+    isave = np.zeros(44, dtype=it)
+    dsave = np.zeros(29, dtype=np.float64)
+    factr = ftol / np.finfo(float).eps
+    seen = None
+    nfev = nit = 0
+    while True:
+        g = g.astype(np.float64)
+        _lbfgsb.setulb(m, x, lb, ub, nbd, f, g, factr, gtol, wa, iwa, task, lsave, isave, dsave, maxls, ln_task)
+        if task[0] == 3:  # f and g at x
+            if seen is None or not np.array_equal(x, seen):
+                seen = x.copy()
+                fv, gv = fg(np.copy(seen))
+                nfev += 1
+            f, g = fv, np.atleast_1d(np.asarray(gv, dtype=np.float64))
+        elif task[0] == 1:  # a new iterate
+            nit += 1
+            if nit >= maxiter:
+                task[0], task[1] = 5, 504
+            elif nfev > maxfun:
+                task[0], task[1] = 5, 502
+        else:
+            break
+    return x
+
+
+_SETULB_OK = None  # None: not checked yet; then True or False
+
+
+def _setulb_usable():
+    """Whether _setulb_loop reproduces scipy.optimize.minimize here: both
+    run once on a fixed bounded fit (a normal CDF fitted to a seeded
+    histogram, as the hot-pixel fit does); any difference or error keeps
+    scipy.optimize.minimize."""
+    global _SETULB_OK
+    if _SETULB_OK is None:
+        try:
+            rng = np.random.default_rng(2024)
+            vals = rng.poisson(20.0, size=200000).astype(np.float64)
+            edges = np.arange(np.floor(20.0 - 7 * np.sqrt(20.0)) - 0.5, np.ceil(20.0 + 7 * np.sqrt(20.0)) + 0.5, 1)
+            hist = np.histogram(vals, bins=edges)[0].astype(np.float64)
+            counts = edges[:-1] + 0.5
+            cdf = np.cumsum(hist) / hist.sum()
+
+            def rows(P):
+                return np.sum(np.abs(cdf[None, :] - scipy.special.ndtr((counts[None, :] - P[:, 0:1]) / P[:, 1:2])),
+                              axis=1)
+
+            s = np.sqrt(20.0)
+            bounds = ((20.0 - 0.5 * s, 20.0 + 0.5 * s), (0.7 * s, 1.3 * s))
+            fg = _value_and_gradient(rows, bounds)
+            ref = scipy.optimize.minimize(fg, (19.3, 1.1 * s), method="L-BFGS-B", bounds=bounds, jac=True).x
+            _SETULB_OK = bool(np.array_equal(_setulb_loop(fg, (19.3, 1.1 * s), bounds), ref))
+        except Exception:
+            _SETULB_OK = False
+    return _SETULB_OK
+
+
+def lbfgsb_minimize(fg, x0, bounds):
+    """x of scipy.optimize.minimize(fg, x0, method='L-BFGS-B', jac=True,
+    bounds=bounds): by the direct loop where it gives scipy's result, else
+    by scipy.optimize.minimize itself."""
+    if _setulb_usable():
+        return _setulb_loop(fg, x0, bounds)
+    return scipy.optimize.minimize(fg, x0, method="L-BFGS-B", bounds=bounds, jac=True).x
+
+
 def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
     """Normal-CDF fit and the outlier cut-offs.  zorro.py:2535-2592.  An empty
     line fit falls back to the configured default, as it did when
@@ -512,11 +604,10 @@ def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
         return np.sum(np.abs(cdf[None, :] - scipy.special.ndtr(z)), axis=1)
 
     bounds = ((sumMean - 0.5 * poissonStd, sumMean + 0.5 * poissonStd), (0.7 * poissonStd, 1.3 * poissonStd))
-    best = scipy.optimize.minimize(_value_and_gradient(err_rows, bounds), (sumMean, poissonStd), method="L-BFGS-B",
-                                   bounds=bounds, jac=True)
+    bx = lbfgsb_minimize(_value_and_gradient(err_rows, bounds), (sumMean, poissonStd), bounds)
     with np.errstate(all="ignore"):
         sig_cdf = np.sqrt(2) * scipy.special.erfinv(2.0 * cdf - 1)
-    normal = (counts - best.x[0]) / best.x[1]
+    normal = (counts - bx[0]) / bx[1]
     e = normal - sig_cdf
     keep = ~np.isinf(e)
     e = e[keep]
@@ -540,7 +631,7 @@ def hotpix_fit(hist, edges, sumMean, poissonStd, hotpixInfo):
             info["cutoffUpper"] = float(cu)
     except IndexError:
         pass
-    return best.x[0], best.x[1], cl, cu, info
+    return bx[0], bx[1], cl, cu, info
 
 
 def psf_kernel(psf="K2"):
