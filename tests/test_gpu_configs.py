@@ -225,15 +225,10 @@ def test_windows_at_crop_2048_maxshift_100(k2_frames):
         assert err < 2e-5, (I, J, err)
 
 
-def test_k2_movie_against_oracle_fixture():
-    """The benchmark's K2 movie itself (40 frames, 780 pairs, hot-pixel and
-    dose filters, even/odd FRC) against its float64 oracle outputs
-    (tests/golden/oracle_k2.npz, made by make_bench_oracle.py): drift and
-    half-set trajectories within 0.01 px, pair measurements, FRC, sampled
-    aligned and dose-filtered sums.  The hot-pixel counts were fitted by the
-    NumPy/SciPy build that made the fixture (its L-BFGS-B can move a pixel
-    that sits on a cut-off); the exact count check at this frame size is the
-    k2x10 case above, against the oracle on this machine."""
+@pytest.fixture(scope="module")
+def k2_movie():
+    """The benchmark's K2 movie and its float64 oracle outputs
+    (tests/golden/oracle_k2.npz, made by make_bench_oracle.py)."""
     from tests.golden.make_bench_oracle import fixture_path
     from tests.golden.make_golden import input_checksum
     path = fixture_path("k2")
@@ -244,12 +239,28 @@ def test_k2_movie_against_oracle_fixture():
     mv = make_movie(**mk)
     if input_checksum(mv["images"]) != str(g["checksum"]):
         pytest.skip("the synthetic K2 movie differs on this platform")
-    reg = gpu_align(mv["raw"], gain=mv["gain"], **attrs)
+    return mv, attrs, g
+
+
+@pytest.mark.parametrize("precision", ["float32", "float16"])
+def test_k2_movie_against_oracle_fixture(k2_movie, precision):
+    """The benchmark's K2 movie itself (40 frames, 780 pairs, hot-pixel and
+    dose filters, even/odd FRC) against its float64 oracle outputs: drift and
+    half-set trajectories within 0.01 px, pair measurements, FRC, sampled
+    aligned and dose-filtered sums; with the frame spectra in float32 and in
+    the mixed-precision form (half-precision spectra with a power-of-two
+    scale each, products, transforms and peaks in float32, the solve in
+    float64).  The hot-pixel counts were fitted by the NumPy/SciPy build that
+    made the fixture (its L-BFGS-B can move a pixel that sits on a cut-off);
+    the exact count check at this frame size is the k2x10 case above,
+    against the oracle on this machine."""
+    mv, attrs, g = k2_movie
+    reg = gpu_align(mv["raw"], gain=mv["gain"], spectraPrecision=precision, **attrs)
     tri = g["corrTriMat"] != 0
     d = np.abs(reg.errorDictList[-1]["shiftsTriMat"] - g["shiftsTriMat"]).max(axis=2)[tri]
     dmax = np.abs(reg.translations - g["translations"]).max()
-    print("k2: %d pairs, %.4f exact; trajectory max %.2e px; even %.2e, odd %.2e" % (
-        tri.sum(), np.mean(d < 1e-9), dmax, np.abs(reg.transEven - g["transEven"]).max(),
+    print("k2 (%s spectra): %d pairs, %.4f exact; trajectory max %.2e px; even %.2e, odd %.2e" % (
+        precision, tri.sum(), np.mean(d < 1e-9), dmax, np.abs(reg.transEven - g["transEven"]).max(),
         np.abs(reg.transOdd - g["transOdd"]).max()))
     assert np.mean(d < 1e-9) >= PAIRS_EXACT
     assert dmax <= TRAJ_TOL

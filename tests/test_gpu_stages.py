@@ -63,6 +63,44 @@ def test_correlation_windows_match_oracle(small, P, C_, mS):
         assert err < 2e-5, (I, J, err)
 
 
+def test_spectra_fill_their_pitch():
+    """Every element of a spectrum buffer is written, the pitch padding of
+    each column (rows C0 + 1 .. C0 + 3) as zeros: zr_pack_half scales each
+    spectrum by its largest element, so stale memory there must not count."""
+    import ctypes as C
+    from tests import gpu_helpers as gh
+    from zorro_gb300 import _lib
+    torch = gh.torch_mod()
+    lib = _lib.load()
+    _lib.call("zr_init", torch.cuda.current_device())
+    P, C_ = (256, 256), (128, 128)
+    mv = make_movie(3, (200, 180), seed=4, mean_dose=1.5, drift_sigma=1.0)
+    raw = gh.dev_tensor(mv["images"].astype(np.float32))
+    fr = gh.frames_of(raw)
+    se = lib.zr_spectrum_elems(C_[0], C_[1])
+    K4 = lib.zr_spectrum_pitch(C_[1])
+    G = torch.full((3, se, 2), 1e30, dtype=torch.float32, device="cuda")
+    S = torch.full((3, se, 2), 1e30, dtype=torch.float32, device="cuda")
+    wb = lib.zr_spectra_work_bytes(200, 3, C_[1])
+    work = torch.full((wb,), 255, dtype=torch.uint8, device="cuda")
+    _lib.call("zr_spectra", C.byref(fr), None, None, 0, 3, 0, P[0], P[1], C_[0], C_[1], G.data_ptr(), S.data_ptr(),
+              work.data_ptr(), wb, gh.stream())
+    torch.cuda.synchronize()
+    for t in (G, S):
+        a = t.cpu().numpy().reshape(3, K4, C_[0] + 4, 2)
+        assert np.isfinite(a).all() and np.abs(a).max() < 1e20
+        assert np.all(a[:, :, C_[0] + 1:, :] == 0.0)
+    # the half-precision scales then come from the spectra themselves
+    G16 = torch.zeros((3, se), dtype=torch.int32, device="cuda")
+    sc = torch.zeros(3, dtype=torch.float32, device="cuda")
+    pw = torch.zeros(16, dtype=torch.uint8, device="cuda")
+    _lib.call("zr_pack_half", G.data_ptr(), 3, se, G16.data_ptr(), sc.data_ptr(), pw.data_ptr(), 16, gh.stream())
+    torch.cuda.synchronize()
+    m = np.abs(G.cpu().numpy().reshape(3, -1)).max(axis=1)
+    s = sc.cpu().numpy()
+    assert np.all(m * s < 2.0 ** 15) and np.all(m * s >= 2.0 ** 14), (m, s)
+
+
 def test_peaks_match_oracle_on_same_windows(small):
     """locatePeak on the GPU vs the oracle, fed the same (GPU) windows."""
     from tests import gpu_helpers as gh

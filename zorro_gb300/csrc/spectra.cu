@@ -164,10 +164,12 @@ __global__ void __launch_bounds__(fft_threads(P0, FC), minb_of(fft_threads(P0, F
   });
   const int hc = C0 / 2;
   const int RP = C0 + 4;
-  for (int e = threadIdx.x; e < (C0 + 1) * FC; e += T) {
-    const int c = e / (C0 + 1), r = e - c * (C0 + 1);
+  // rows C0 + 1 .. C0 + 3 pad the column to its pitch: written as zeros, so
+  // that every element of a spectrum is defined (zr_pack_half scans them all)
+  for (int e = threadIdx.x; e < RP * FC; e += T) {
+    const int c = e / RP, r = e - c * RP;
     const int ky = r < hc ? r : (r < C0 ? P0 - C0 + r : hc);
-    out[(size_t)(k0 + c) * RP + r] = sm[c * LD + pidx(ky)];
+    out[(size_t)(k0 + c) * RP + r] = r <= C0 ? sm[c * LD + pidx(ky)] : make_float2(0.0f, 0.0f);
   }
 }
 
