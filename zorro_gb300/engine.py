@@ -1212,7 +1212,10 @@ class Engine:
         out["hotpixInfo"] = hotinfo
         out["shapeOriginal"] = [H, W]
         out["pixelsize"] = pixelsize
-        out["masks"] = np.ones([1, H, W], dtype=bool) if not user_mask else reg.masks
+        if user_mask:
+            out["masks"] = reg.masks
+        else:
+            out["_ones_mask_shape"] = (H, W)  # the all-true mask, made when the registrator's masks are read
         bench["align1"] = time.time()
         b = dict(reg.bench)
         b.update(bench)

@@ -285,6 +285,23 @@ class ImageRegistrator:
             a = a.detach().cpu().numpy()
         return np.asarray(a)
 
+    @property
+    def masks(self):
+        """The registration mask (None: the whole frame).  After a registration
+        without one this is the all-true [1, H, W] mask the reference leaves
+        (zorro.py:584-586), made when first read rather than for every
+        movie."""
+        m = self.__dict__.get("_masks")
+        if m is None and self.__dict__.get("_ones_mask_shape") is not None:
+            H, W = self._ones_mask_shape
+            m = self._masks = np.ones([1, H, W], dtype=bool)
+        return m
+
+    @masks.setter
+    def masks(self, v):
+        self._masks = v
+        self._ones_mask_shape = None
+
     def alignImageStack(self):
         """Register and sum the stack.  zorro.py:1569-1716."""
         if str(self.xcorrMode).lower() != "zorro":
@@ -315,8 +332,8 @@ def alignImageStacks(registrators, device=None):
 def copy_config(src, dst):
     """Copy the registration attributes of one registrator to another."""
     for k, v in vars(src).items():
-        if k in ("images", "imageSum", "filtSum", "gainRef", "masks", "errorDictList", "FRC", "FRC2D",
-                 "translations", "files", "imagesAreRaw"):
+        if k in ("images", "imageSum", "filtSum", "gainRef", "masks", "_masks", "_ones_mask_shape", "errorDictList",
+                 "FRC", "FRC2D", "translations", "files", "imagesAreRaw"):
             continue
         setattr(dst, k, copy.deepcopy(v))
     return dst
