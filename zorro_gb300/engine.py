@@ -198,6 +198,16 @@ class Engine:
                 st = self._slots[slot] = {"bufs": {}, "stream": stream, "key": slot}
             return st
 
+    def _copy_stream(self):
+        """A stream of the current slot for copies that may overlap its
+        kernels (made on first use)."""
+        st = getattr(self._tls, "slot", None) or self._slot(0)
+        with self._slots_lock:
+            s = st.get("copy")
+            if s is None:
+                s = st["copy"] = self.torch.cuda.Stream(device=self.dev)
+            return s
+
     @property
     def bufs(self):
         st = getattr(self._tls, "slot", None)
@@ -1131,6 +1141,26 @@ class Engine:
                 self.call("I_dose", "zr_dose_filter", aligned.data_ptr(), N, H, W, C.byref(dp), tq.data_ptr(), de.data_ptr(),
                           P0, P1, filt_sum.data_ptr(), self.ptr(pfx + "dosework", dwb), dwb, st)
         bench["dose1"] = time.time()
+        # host results: the sums are final now, so their copies to pinned host
+        # memory go on a side stream at once, behind the kernels that make
+        # them, and overlap what follows (the half-set registrations)
+        early = {}
+        if not bool(getattr(reg, "returnDeviceArrays", False)):
+            made = torch.cuda.Event()
+            made.record()
+            side = self._copy_stream()
+            side.wait_event(made)
+            with torch.cuda.stream(side):
+                for k, t in (("imageSum", isum), ("filtSum", filt_sum)):
+                    if t is not None:
+                        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+                        h.copy_(t, non_blocking=True)
+                        early[k] = h
+            if early:
+                copied = torch.cuda.Event()
+                copied.record(side)
+                early[None] = copied
+        job.early = early
         if finish_errors is not None:  # while the GPU shifts, sums and filters
             finish_errors()
             ed["originTriMat"] = orig
@@ -1195,12 +1225,16 @@ class Engine:
             pending.append(h)
             return h
 
-        out["imageSum"] = fetch(isum)
+        early = getattr(job, "early", None) or {}
+        if early:
+            torch.cuda.current_stream(self.dev).wait_event(early[None])
+            pending.extend(v for k, v in early.items() if k is not None)
+        out["imageSum"] = early["imageSum"] if "imageSum" in early else fetch(isum)
         if frc is not None:
             out["FRC"] = fetch(frc)
             out["FRC2D"] = fetch(frc2d)
         if filt_sum is not None:
-            out["filtSum"] = fetch(filt_sum)
+            out["filtSum"] = early["filtSum"] if "filtSum" in early else fetch(filt_sum)
         if reg.keepAlignedImages:
             out["images"] = fetch(aligned)
             out["imagesAreRaw"] = False
